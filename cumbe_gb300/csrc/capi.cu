@@ -1,0 +1,223 @@
+// C ABI of libmbe: contexts, device residency, enumeration, batching.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "engine_host.h"
+#include "graph_dev.cuh"
+#include "mbe_internal.h"
+
+using namespace mbe;
+
+struct mbe_ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    std::unordered_map<uint64_t, DeviceGraph> resident;
+    EngineBuffers eb;
+    EngineStats last_stats;
+    std::mutex mu;
+};
+
+namespace {
+
+mbe_status check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return MBE_OK;
+    cudaGetLastError();
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return fail(MBE_ERR_NO_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(e == cudaErrorMemoryAllocation ? MBE_ERR_OUT_OF_MEMORY : MBE_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+mbe_status ensure_resident(mbe_ctx* ctx, const mbe_graph* g, const DeviceGraph** out) {
+    auto it = ctx->resident.find(g->uid);
+    if (it != ctx->resident.end()) {
+        *out = &it->second;
+        return MBE_OK;
+    }
+    DeviceGraph d;
+    mbe_status st = build_device_graph(g, ctx->stream, ctx->n_sm, &d);
+    if (st != MBE_OK) return st;
+    auto res = ctx->resident.emplace(g->uid, std::move(d));
+    *out = &res.first->second;
+    return MBE_OK;
+}
+
+EngineConfig make_config(mbe_variant v, const mbe_opts* o, bool swapped) {
+    EngineConfig c;
+    c.variant = (uint32_t)v;
+    if (o) {
+        // thresholds are given in file orientation (rows/cols)
+        c.minL = swapped ? o->min_rows : o->min_cols;
+        c.minR = swapped ? o->min_cols : o->min_rows;
+        if (o->donate_min) c.donate_min = o->donate_min;
+        if (o->blocks_per_sm) c.blocks_per_sm = o->blocks_per_sm;
+        if (o->stack_words) c.arena_words = (o->stack_words + 3u) & ~3u;
+    }
+    if (const char* env = std::getenv("MBE_POOL_MB")) {
+        unsigned long long mb = std::strtoull(env, nullptr, 10);
+        if (mb) c.pool_words = mb * (1ull << 20) / 4;
+    }
+    return c;
+}
+
+}  // namespace
+
+extern "C" mbe_status mbe_ctx_create(int device, mbe_ctx** out) {
+    clear_error();
+    if (!out) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    int n = 0;
+    mbe_status st = check_cuda(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (st != MBE_OK) return st;
+    if (device < 0 || device >= n) return fail(MBE_ERR_NO_DEVICE, "device index out of range");
+    if ((st = check_cuda(cudaSetDevice(device), "cudaSetDevice"))) return st;
+    auto* c = new (std::nothrow) mbe_ctx();
+    if (!c) return fail(MBE_ERR_OUT_OF_MEMORY, "host allocation failed");
+    c->device = device;
+    if ((st = check_cuda(cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device), "attr")) ||
+        (st = check_cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate"))) {
+        delete c;
+        return st;
+    }
+    *out = c;
+    return MBE_OK;
+}
+
+extern "C" void mbe_ctx_destroy(mbe_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->resident) kv.second.release();
+    ctx->eb.release();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" mbe_status mbe_graph_upload(mbe_ctx* ctx, const mbe_graph* g) {
+    clear_error();
+    if (!ctx || !g) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (st) return st;
+    const DeviceGraph* d;
+    return ensure_resident(ctx, g, &d);
+}
+
+extern "C" mbe_status mbe_graph_release(mbe_ctx* ctx, const mbe_graph* g) {
+    clear_error();
+    if (!ctx || !g) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->resident.find(g->uid);
+    if (it != ctx->resident.end()) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        it->second.release();
+        ctx->resident.erase(it);
+    }
+    return MBE_OK;
+}
+
+static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
+                             const mbe_opts* opts, mbe_result* out, float* total_ms) {
+    if (opts && (opts->flags & MBE_OPT_EMIT))
+        return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT is not supported by this build");
+    mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (st) return st;
+    std::vector<const DeviceGraph*> devs(n);
+    bool any_swapped = false, any_plain = false;
+    for (uint32_t i = 0; i < n; i++) {
+        if (!graphs[i]) return fail(MBE_ERR_INVALID_ARG, "null graph");
+        if ((st = ensure_resident(ctx, graphs[i], &devs[i]))) return st;
+        (devs[i]->swapped ? any_swapped : any_plain) = true;
+    }
+    // Roots, heaviest first (rank order is degree order within a graph).
+    std::vector<uint2> roots;
+    size_t total = 0;
+    for (uint32_t i = 0; i < n; i++) total += devs[i]->nR - devs[i]->n_isolated;
+    roots.reserve(total);
+    for (uint32_t i = 0; i < n; i++)
+        for (uint32_t r = devs[i]->nR; r-- > devs[i]->n_isolated;) roots.push_back(make_uint2(i, r));
+    if (n > 1)
+        std::stable_sort(roots.begin(), roots.end(), [&](const uint2& a, const uint2& b) {
+            return devs[a.x]->deg_by_rank[a.y] > devs[b.x]->deg_by_rank[b.y];
+        });
+    // Thresholds are stated in file orientation; a batch mixing orientations
+    // is enumerated per orientation group.
+    std::vector<ResultAcc> acc(n, ResultAcc{0, 0, 0, 0});
+    float ms = 0;
+    EngineStats stats;
+    bool thresholds = opts && (opts->min_rows || opts->min_cols);
+    for (int pass = 0; pass < 2; pass++) {
+        bool sw = pass == 1;
+        if (sw ? !any_swapped : !any_plain) continue;
+        std::vector<uint2> sel;
+        if (thresholds && any_swapped && any_plain) {
+            for (const uint2& r : roots)
+                if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
+        }
+        const std::vector<uint2>& use = (thresholds && any_swapped && any_plain) ? sel : roots;
+        EngineConfig cfg = make_config(variant, opts, sw);
+        std::vector<ResultAcc> part;
+        EngineStats ps;
+        st = engine_run(ctx->eb, ctx->stream, cfg, devs, use, part, &ps);
+        if (st != MBE_OK) return st;
+        for (uint32_t i = 0; i < n; i++) {
+            acc[i].count += part[i].count;
+            acc[i].hash += part[i].hash;
+            acc[i].nodes += part[i].nodes;
+            acc[i].words += part[i].words;
+        }
+        ms += ps.ms_expand + ps.ms_dfs;
+        stats.ms_expand += ps.ms_expand;
+        stats.ms_dfs += ps.ms_dfs;
+        stats.chunks += ps.chunks;
+        stats.grid_a = ps.grid_a;
+        stats.grid_b = ps.grid_b;
+        if (!(thresholds && any_swapped && any_plain)) break;
+    }
+    ctx->last_stats = stats;
+    for (uint32_t i = 0; i < n; i++) {
+        mbe_result& r = out[i];
+        std::memset(&r, 0, sizeof r);
+        r.count = acc[i].count;
+        r.hash = (opts && (opts->flags & MBE_OPT_NO_HASH)) ? 0 : acc[i].hash;
+        r.nodes = acc[i].nodes;
+        r.words = acc[i].words;
+        r.ms = stats.ms_expand + stats.ms_dfs;
+        r.ms_prep = stats.ms_expand;
+    }
+    if (total_ms) *total_ms = ms;
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_enumerate(mbe_ctx* ctx, const mbe_graph* g, mbe_variant variant, const mbe_opts* opts,
+                                    mbe_result* out) {
+    clear_error();
+    if (!ctx || !g || !out) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return run_graphs(ctx, &g, 1, variant, opts, out, nullptr);
+}
+
+extern "C" mbe_status mbe_batch_run(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
+                                    const mbe_opts* opts, mbe_result* out, float* total_ms) {
+    clear_error();
+    if (!ctx || (!graphs && n) || (!out && n)) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return run_graphs(ctx, graphs, n, variant, opts, out, total_ms);
+}
+
+// Launch geometry of the last enumeration (CLI "grid_size" line).
+extern "C" mbe_status mbe_ctx_last_grid(mbe_ctx* ctx, uint32_t* grid_expand, uint32_t* grid_dfs, uint32_t* block) {
+    clear_error();
+    if (!ctx) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    if (grid_expand) *grid_expand = ctx->last_stats.grid_a;
+    if (grid_dfs) *grid_dfs = ctx->last_stats.grid_b;
+    if (block) *block = 256;
+    return MBE_OK;
+}

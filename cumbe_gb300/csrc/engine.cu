@@ -1,0 +1,1301 @@
+// Enumeration kernels (sm_103a) and their host driver.
+//
+// Reference path replaced: CUDA_MBE_cuMBE / noES / noRS / noWS
+// (src/mbe_cuMBE.cuh, src/mbe_noES.cuh, src/mbe_noRS.cuh, src/mbe_noWS.cuh)
+// and the per-block state plan around them (src/main.cu:72-119,
+// src/global_extension.cuh).  The reference runs one tree node per
+// 512-thread block with __syncthreads between every step, serial
+// thread-0 partition loops, an O(|R|) P reset per root and grid-wide
+// barriers for stealing.  Here:
+//   - expand_roots_kernel (one block per root, persistent): builds the
+//     root's bit-row universe by reverse scanning N(N(x)) (the reference's
+//     RS, src/mbe_cuMBE.cuh:215-263), tests root maximality, counts the
+//     root biclique and publishes the root's record as a task;
+//   - dfs_kernel (one warp per task, persistent): depth-first search over
+//     node records with popcount intersections, no block barriers, and
+//     work donation to hungry warps through a device task queue (the
+//     reference's level-1 stealing, src/mbe_cuMBE.cuh:570-621,1208-1256,
+//     generalised to any depth).  Termination is an outstanding-task
+//     counter, not a grid barrier; every wait is bounded by %globaltimer.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "engine.cuh"
+#include "engine_host.h"
+#include "mbe_hash.h"
+
+namespace mbe {
+
+namespace {
+
+constexpr int kThreadsA = 256;
+constexpr int kWarpsB = 8;
+constexpr int kThreadsB = kWarpsB * 32;
+constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
+constexpr unsigned long long kInvalidKey = ~0ull;
+constexpr uint32_t kKeepWindow = 32;     // Q rows a dropped Q row is tested against
+
+__device__ __forceinline__ void set_error(const EngineArgs& a, int code, unsigned long long info) {
+    if (atomicCAS(a.error, 0, code) == 0) *a.error_info = info;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
+    return *(const volatile unsigned long long*)p;
+}
+
+// Publishes a task in the ring.  pending is raised before the slot becomes
+// visible so that pending == 0 implies no queued and no running task.
+// Callers leave q_margin slots free (donors check before calling; the root
+// expansion pushes at most n_roots <= capacity - margin), so the slot of
+// ticket t was released by the consumer of ticket t - capacity long ago;
+// the wait below is a bounded guard, never expected to spin.
+__device__ bool push_task(const EngineArgs& a, Task t) {
+    atomicAdd(a.pending, 1);
+    uint32_t tk = atomicAdd(a.q_tail, 1u);
+    uint32_t slot = tk % a.task_cap;
+    unsigned long long t0 = 0;
+    while (ld_volatile(&a.ready[slot]) != 0) {
+        if (t0 == 0) t0 = globaltimer_ns();
+        if (globaltimer_ns() - t0 > 1000000000ull) {
+            set_error(a, kErrQueue, tk);
+            atomicSub(a.pending, 1);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    volatile Task* dst = (volatile Task*)&a.tasks[slot];
+    dst->node = t.node;
+    dst->begin = t.begin;
+    dst->end = t.end;
+    dst->plen = t.plen;
+    for (uint32_t j = 0; j < t.plen && j < kMaxPath; j++) dst->path[j] = t.path[j];
+    __threadfence();
+    atomicExch(&a.ready[slot], tk + 1u);
+    return true;
+}
+
+// Bump allocation from the node pool; ~0 when it does not fit.  Sizes are
+// rounded to 128-byte lines so that records written by one SM and read by
+// another never share a cache line with a record read earlier (L1 is not
+// coherent across SMs).
+__device__ unsigned long long pool_alloc(const EngineArgs& a, unsigned long long words) {
+    words = (words + 31) & ~31ull;
+    unsigned long long old = ld_volatile(a.pool_top);
+    for (;;) {
+        if (old + words > a.pool_words) return ~0ull;
+        unsigned long long prev = atomicCAS(a.pool_top, old, old + words);
+        if (prev == old) return old;
+        old = prev;
+    }
+}
+
+__device__ __forceinline__ uint64_t side_hash(const GraphView& G, uint64_t sL, uint32_t nl, uint64_t sR,
+                                              uint32_t nr) {
+    // A = rows, B = cols of the file; R is the file's rows unless swapped.
+    return G.swapped ? mbe_pair_hash(sL, nl, sR, nr) : mbe_pair_hash(sR, nr, sL, nl);
+}
+
+// ---------------------------------------------------------------------------
+// block-level bitonic sort of u64 keys (n a power of two)
+
+__device__ void block_sort_u64(unsigned long long* k, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1)
+        for (uint32_t j = size >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    unsigned long long x = k[i], y = k[ixj];
+                    bool asc = (i & size) == 0;
+                    if ((x > y) == asc) {
+                        k[i] = y;
+                        k[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// warp-level bitonic sort of u64 keys in memory (n a power of two >= 32)
+__device__ void warp_sort_u64(unsigned long long* k, uint32_t n) {
+    unsigned lane = lane_id();
+    for (uint32_t size = 2; size <= n; size <<= 1)
+        for (uint32_t j = size >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < n; i += 32) {
+                uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    unsigned long long x = k[i], y = k[ixj];
+                    bool asc = (i & size) == 0;
+                    if ((x > y) == asc) {
+                        k[i] = y;
+                        k[ixj] = x;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
+// register bitonic sort across the 32 lanes (ascending by lane)
+__device__ __forceinline__ unsigned long long warp_sort_reg(unsigned long long v) {
+    unsigned lane = lane_id();
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+        for (int j = size >> 1; j > 0; j >>= 1) {
+            unsigned long long o = __shfl_xor_sync(kFull, v, j);
+            bool up = (lane & size) == 0, lower = (lane & j) == 0;
+            v = (lower == up) ? (v < o ? v : o) : (v > o ? v : o);
+        }
+    return v;
+}
+
+__device__ __forceinline__ uint32_t next_pow2(uint32_t x) {
+    uint32_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// Phase A: root expansion
+
+__global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
+    __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax;
+    __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
+    __shared__ unsigned long long s_sabs, s_sl, s_rec, s_scan;
+    __shared__ unsigned long long s_keys[2048];
+    int* cmap = a.cmap + (size_t)blockIdx.x * a.maxNR;
+    uint32_t* cl = a.a_cl + (size_t)blockIdx.x * a.maxNR;
+    uint32_t* cntA = a.a_cnt + (size_t)blockIdx.x * a.maxNR;
+    unsigned long long* gkeys = a.a_keys + (size_t)blockIdx.x * a.keys_cap;
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nwarps = blockDim.x >> 5;
+    const bool rs = a.variant != MBE_NORS;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_stop = 0;
+            if (ld_volatile(a.error))
+                s_stop = 1;
+            else if (ld_volatile(a.pool_top) > a.pool_watermark)
+                s_stop = 1;
+            else {
+                uint32_t i = atomicAdd(a.root_next, 1u);
+                if (i >= a.n_roots)
+                    s_stop = 1;
+                else
+                    s_idx = i;
+            }
+            s_ncand = 0;
+            s_nq = s_np = s_nabs = s_nonmax = 0;
+            s_sabs = s_sl = s_scan = 0;
+        }
+        __syncthreads();
+        if (s_stop) break;
+        const uint2 rt = a.roots[s_idx];
+        const GraphView G = a.graphs[rt.x];
+        const uint32_t x = rt.y;
+        const uint32_t d = G.r_ptr[x + 1] - G.r_ptr[x];
+        if (d == 0 || d < a.minL) continue;  // uniform across the block
+        const uint32_t* L0 = G.r_adj + G.r_ptr[x];
+        const uint32_t W = (d + 31) / 32;
+
+        // 1. candidates C = N(N(x)) \ {x}: first toucher claims a slot
+        unsigned long long scan = 0;
+        for (uint32_t j = warp; j < d; j += nwarps) {
+            uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+            scan += e - b;
+            for (uint32_t k = b + lane; k < e; k += 32) {
+                uint32_t v = G.l_adj[k];
+                if (v != x && atomicCAS(&cmap[v], -1, -2) == -1) cl[atomicAdd(&s_ncand, 1u)] = v;
+            }
+        }
+        __syncthreads();
+        const uint32_t n = s_ncand;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            cmap[cl[i]] = (int)i;
+            cntA[i] = 0;
+        }
+        __syncthreads();
+        // 2. |N(v) n L0| per candidate
+        if (rs) {
+            // reverse scan: scatter from every u in L0 (src/mbe_cuMBE.cuh:215-227)
+            for (uint32_t j = warp; j < d; j += nwarps) {
+                uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+                for (uint32_t k = b + lane; k < e; k += 32) {
+                    uint32_t v = G.l_adj[k];
+                    if (v != x) atomicAdd(&cntA[cmap[v]], 1u);
+                }
+            }
+        } else {
+            // forward scan: each candidate's own list against sorted L0
+            // (src/mbe_noRS.cuh:274-283)
+            for (uint32_t i = warp; i < n; i += nwarps) {
+                uint32_t v = cl[i], b = G.r_ptr[v], e = G.r_ptr[v + 1];
+                uint32_t c = 0;
+                for (uint32_t k = b + lane; k < e; k += 32) {
+                    uint32_t u = G.r_adj[k], lo = 0, hi = d;
+                    while (lo < hi) {
+                        uint32_t mid = (lo + hi) >> 1;
+                        if (L0[mid] < u)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
+                    }
+                    c += (lo < d && L0[lo] == u);
+                }
+                scan += e - b;
+                c = warp_sum(c);
+                if (lane == 0) cntA[i] = c;
+            }
+        }
+        __syncthreads();
+        // 3. classify: Q part (lower rank), absorbed, P part
+        unsigned long long sabs = 0;
+        uint32_t nabs = 0, nq = 0, np = 0, nonmax = 0;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            uint32_t v = cl[i], c = cntA[i];
+            unsigned long long key;
+            if (v < x) {
+                nonmax |= (c == d);
+                key = ((unsigned long long)(0x7FFFFFFFu - c) << 32) | v;  // count desc, rank asc
+                nq++;
+            } else if (c == d) {
+                key = kInvalidKey;
+                sabs += G.eR[v];
+                nabs++;
+                cmap[v] = -3;
+            } else {
+                key = (1ull << 63) | ((unsigned long long)c << 32) | v;
+                np++;
+            }
+            if (n <= 2048)
+                s_keys[i] = key;
+            else
+                gkeys[i] = key;
+        }
+        sabs = warp_sum(sabs);
+        nabs = warp_sum(nabs);
+        nq = warp_sum(nq);
+        np = warp_sum(np);
+        nonmax = __any_sync(kFull, nonmax != 0);
+        scan = warp_sum(scan);
+        unsigned long long sl = 0;
+        for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) sl += G.eL[L0[j]];
+        sl = warp_sum(sl);
+        if (lane == 0) {
+            atomicAdd(&s_sabs, sabs);
+            atomicAdd(&s_nabs, nabs);
+            atomicAdd(&s_nq, nq);
+            atomicAdd(&s_np, np);
+            if (nonmax) s_nonmax = 1;
+            atomicAdd(&s_sl, sl);
+            atomicAdd(&s_scan, scan);
+        }
+        __syncthreads();
+        const uint32_t nRset = 1 + s_nabs;
+        const uint32_t n2 = s_nq + s_np;
+        const bool emit_task = !s_nonmax && s_np > 0 && nRset + s_np >= a.minR;
+        const uint64_t rw = record_words(W, n2);
+        if (threadIdx.x == 0) {
+            s_rec = ~0ull;
+            bool ok = true;
+            if (emit_task) {
+                unsigned long long off = pool_alloc(a, rw);
+                if (off == ~0ull) {
+                    // does not fit this chunk: retry in a later chunk, count nothing now
+                    ok = false;
+                    uint32_t r = atomicAdd(a.n_retry, 1u);
+                    if (r < a.retry_cap)
+                        a.retry[r] = s_idx;
+                    else
+                        set_error(a, kErrPool, rw);
+                }
+                s_rec = off;
+            }
+            if (ok) {
+                ResultAcc* r = &a.results[rt.x];
+                unsigned long long words = s_scan * (rs ? 3 : 2) + d;
+                atomicAdd(&r->nodes, 1ull);
+                atomicAdd(&r->words, words);
+                if (!s_nonmax && nRset >= a.minR) {
+                    unsigned long long sR = G.eR[x] + s_sabs;
+                    atomicAdd(&r->count, 1ull);
+                    atomicAdd(&r->hash, (unsigned long long)side_hash(G, s_sl, d, sR, nRset));
+                }
+            }
+        }
+        __syncthreads();
+        if (emit_task && s_rec != ~0ull) {
+            // 4. order: Q part by rank, then P part by (count, rank)
+            uint32_t N = next_pow2(max(n, 2u));
+            unsigned long long* keys = (n <= 2048 && N <= 2048) ? s_keys : gkeys;
+            if (keys == gkeys && n <= 2048)
+                for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) gkeys[i] = s_keys[i];
+            for (uint32_t i = n + threadIdx.x; i < N; i += blockDim.x) keys[i] = kInvalidKey;
+            __syncthreads();
+            block_sort_u64(keys, N);
+            {
+                uint32_t* rec = a.pool + s_rec;
+                uint32_t* wmap = rec + kHdrWords;
+                uint32_t* Lm = wmap + pad4(W);
+                uint32_t* cand = Lm + pad4(W);
+                uint32_t* cnt = cand + pad4(n2);
+                uint32_t* M = cnt + pad4(n2);
+                if (threadIdx.x == 0) {
+                    atomicMax(a.max_n, n2);
+                    NodeHdr* h = (NodeHdr*)rec;
+                    h->graph = rt.x;
+                    h->root = x;
+                    h->W = W;
+                    h->n = n2;
+                    h->nq = s_nq;
+                    h->l = d;
+                    h->nRset = nRset;
+                    h->depth = 1;
+                    h->sR = G.eR[x] + s_sabs;
+                    h->words = (uint32_t)rw;
+                    h->rlist = 0;
+                }
+                for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
+                    wmap[w] = w;
+                    uint32_t rem = d - w * 32;
+                    Lm[w] = rem >= 32 ? 0xFFFFFFFFu : ((1u << rem) - 1u);
+                }
+                for (uint32_t p = threadIdx.x; p < n2; p += blockDim.x) {
+                    unsigned long long k = keys[p];
+                    uint32_t v = (uint32_t)k;
+                    cand[p] = v;
+                    cnt[p] = (k >> 63) ? (uint32_t)((k >> 32) & 0x7FFFFFFFu) : 0u;
+                    cmap[v] = (int)p;
+                }
+                uint64_t mw = (uint64_t)W * n2;
+                for (uint64_t i = threadIdx.x; i < mw; i += blockDim.x) M[i] = 0;
+                __syncthreads();
+                // 6. bit rows: bit j of candidate p set iff (L0[j], cand[p]) is an edge
+                if (rs) {
+                    for (uint32_t j = warp; j < d; j += nwarps) {
+                        uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+                        uint32_t* Mw = M + (size_t)(j >> 5) * n2;
+                        uint32_t bit = 1u << (j & 31);
+                        for (uint32_t k = b + lane; k < e; k += 32) {
+                            int p = cmap[G.l_adj[k]];
+                            if (p >= 0) atomicOr(&Mw[p], bit);
+                        }
+                    }
+                } else {
+                    for (uint32_t p = warp; p < n2; p += nwarps) {
+                        uint32_t v = cand[p], b = G.r_ptr[v], e = G.r_ptr[v + 1];
+                        for (uint32_t k = b + lane; k < e; k += 32) {
+                            uint32_t u = G.r_adj[k], lo = 0, hi = d;
+                            while (lo < hi) {
+                                uint32_t mid = (lo + hi) >> 1;
+                                if (L0[mid] < u)
+                                    lo = mid + 1;
+                                else
+                                    hi = mid;
+                            }
+                            if (lo < d && L0[lo] == u) atomicOr(&M[(size_t)(lo >> 5) * n2 + p], 1u << (lo & 31));
+                        }
+                    }
+                }
+                __syncthreads();
+                // 7. Q reduction: a Q row contained in one of the first
+                // kKeepWindow kept rows (Q is in count-descending order) is
+                // dropped; the record is then compacted in place.
+                uint32_t* flag = (uint32_t*)keys;  // keys are consumed: reuse as keep flags
+                if (warp == 0) {
+                    uint32_t kept_p = 0, nk = 0, pos = 0;
+                    while (pos < s_nq && nk < kKeepWindow) {
+                        bool dom = false;
+                        if (lane < nk) {
+                            dom = true;
+                            for (uint32_t w = 0; w < W && dom; w++) {
+                                const uint32_t* Mw = M + (size_t)w * n2;
+                                if (Mw[pos] & ~Mw[kept_p]) dom = false;
+                            }
+                        }
+                        bool keep = !__any_sync(kFull, dom);
+                        if (keep && lane == nk) kept_p = pos;
+                        if (lane == 0) flag[pos] = keep;
+                        nk += keep;
+                        pos++;
+                    }
+                    if (lane < nk) s_kept[lane] = kept_p;
+                    if (lane == 0) {
+                        s_nk = nk;
+                        s_p1 = pos;
+                    }
+                }
+                __syncthreads();
+                for (uint32_t p = s_p1 + threadIdx.x; p < s_nq; p += blockDim.x) {
+                    bool keep = true;
+                    for (uint32_t j = 0; j < s_nk && keep; j++) {
+                        uint32_t kp = s_kept[j];
+                        bool sub = true;
+                        for (uint32_t w = 0; w < W && sub; w++) {
+                            const uint32_t* Mw = M + (size_t)w * n2;
+                            if (Mw[p] & ~Mw[kp]) sub = false;
+                        }
+                        if (sub) keep = false;
+                    }
+                    flag[p] = keep;
+                }
+                __syncthreads();
+                // new positions of kept Q rows (block scan in chunks)
+                if (threadIdx.x == 0) s_nq2 = 0;
+                __syncthreads();
+                for (uint32_t b0 = 0; b0 < s_nq; b0 += blockDim.x) {
+                    uint32_t p = b0 + threadIdx.x;
+                    uint32_t f = p < s_nq ? flag[p] : 0u;
+                    unsigned bal = __ballot_sync(kFull, f);
+                    if (lane == 0) s_wsum[warp] = __popc(bal);
+                    __syncthreads();
+                    uint32_t before = s_nq2;
+                    for (uint32_t ww = 0; ww < warp; ww++) before += s_wsum[ww];
+                    if (p < s_nq) flag[p] = f ? (before + __popc(bal & lanemask_lt())) : 0xFFFFFFFFu;
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        uint32_t tot = 0;
+                        for (uint32_t ww = 0; ww < nwarps; ww++) tot += s_wsum[ww];
+                        s_nq2 += tot;
+                    }
+                    __syncthreads();
+                }
+                const uint32_t nq2 = s_nq2;
+                if (nq2 < s_nq) {
+                    const uint32_t n3 = nq2 + s_np;
+                    // every move goes to a lower address: process arrays in
+                    // address order, each in chunks read-all-then-write-all
+                    auto newpos = [&](uint32_t p) -> uint32_t {
+                        return p < s_nq ? flag[p] : p - s_nq + nq2;
+                    };
+                    uint32_t* cand3 = Lm + pad4(W);
+                    uint32_t* cnt3 = cand3 + pad4(n3);
+                    uint32_t* M3 = cnt3 + pad4(n3);
+                    for (int arr = 0; arr < 2 + (int)W; arr++) {
+                        const uint32_t* src = arr == 0 ? cand : arr == 1 ? cnt : M + (size_t)(arr - 2) * n2;
+                        uint32_t* dst = arr == 0 ? cand3 : arr == 1 ? cnt3 : M3 + (size_t)(arr - 2) * n3;
+                        for (uint32_t b0 = 0; b0 < n2; b0 += 4 * blockDim.x) {
+                            uint32_t vals[4], dpos[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                uint32_t p = b0 + q * blockDim.x + threadIdx.x;
+                                dpos[q] = 0xFFFFFFFFu;
+                                if (p < n2) {
+                                    uint32_t np_ = newpos(p);
+                                    if (np_ != 0xFFFFFFFFu) {
+                                        dpos[q] = np_;
+                                        vals[q] = src[p];
+                                    }
+                                }
+                            }
+                            __syncthreads();
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                if (dpos[q] != 0xFFFFFFFFu) dst[dpos[q]] = vals[q];
+                            __syncthreads();
+                        }
+                    }
+                    if (threadIdx.x == 0) {
+                        NodeHdr* h = (NodeHdr*)rec;
+                        h->n = n3;
+                        h->nq = nq2;
+                        h->words = (uint32_t)record_words(W, n3);
+                    }
+                }
+                __threadfence();
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    Task t{};
+                    t.node = (unsigned long long)(rec);
+                    t.begin = 0;
+                    t.end = s_np;
+                    t.plen = 0;  // pool record: shared by pointer
+                    push_task(a, t);
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) cmap[cl[i]] = -1;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase B: warp DFS with donation
+
+struct WarpCtx {
+    uint32_t* arena;
+    uint32_t arena_top;
+    uint32_t* scrLi;
+    uint32_t* scrNz;
+    uint32_t* scrQcnt;
+    unsigned long long* scrKeysP;
+    unsigned long long* scrKeysQ;
+    uint32_t* sLi;
+    uint32_t* sNz;
+};
+
+// Ticket queue: an idle warp takes the next slot index with one atomicAdd
+// and then watches only that slot's ready flag, so waiting warps never
+// contend on a shared word.  Slot h is filled by the h-th push.  Waiting
+// ends when the slot is ready, or when pending == 0 (no queued and no
+// running task: nothing can be pushed any more), or on an error, or when
+// no warp has made progress for timeout_ns.
+__device__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my_path) {
+    unsigned lane = lane_id();
+    int state = 0;  // 1 = got, 2 = done
+    uint32_t h = 0;
+    if (lane == 0) {
+        h = atomicAdd(a.q_head, 1u);
+        unsigned long long t0 = globaltimer_ns();
+        unsigned long long last_prog = ld_volatile(a.progress);
+        unsigned sleep_ns = 32;
+        const uint32_t slot = h % a.task_cap;
+        for (;;) {
+            if (ld_volatile(&a.ready[slot]) == h + 1u) {
+                state = 1;
+                break;
+            }
+            if (ld_volatile(a.error) || ld_volatile(a.pending) == 0) {
+                state = 2;
+                break;
+            }
+            __nanosleep(sleep_ns);
+            if (sleep_ns < 1024) sleep_ns <<= 1;
+            unsigned long long now = globaltimer_ns();
+            unsigned long long prog = ld_volatile(a.progress);
+            if (prog != last_prog) {
+                last_prog = prog;
+                t0 = now;
+            } else if (now - t0 > a.timeout_ns) {
+                set_error(a, kErrTimeout, h);
+                state = 2;
+                break;
+            }
+        }
+        __threadfence();
+    }
+    state = __shfl_sync(kFull, state, 0);
+    h = __shfl_sync(kFull, h, 0);
+    if (state != 1) return false;
+    const uint32_t slot = h % a.task_cap;
+    volatile Task* src = (volatile Task*)&a.tasks[slot];
+    t.node = src->node;
+    t.begin = src->begin;
+    t.end = src->end;
+    t.plen = src->plen;
+    my_path = lane < t.plen ? src->path[lane] : 0u;  // lane j holds path[j]
+    __syncwarp();
+    if (lane == 0) {
+        __threadfence();
+        atomicExch(&a.ready[slot], 0u);
+        atomicAdd(a.q_done, 1u);
+    }
+    return true;
+}
+
+struct ChildOut {
+    uint32_t* rec;
+    uint32_t nchild;
+    uint32_t size;   // words taken from the arena (0 when in the pool)
+};
+
+
+// row(c) n L_i is a subset of row(k) (both within the non-zero words of L_i)
+__device__ __forceinline__ bool row_subset(const uint32_t* M, uint32_t n, const uint32_t* Nz, const uint32_t* Li,
+                                           uint32_t nnz, uint32_t c, uint32_t k) {
+    for (uint32_t j = 0; j < nnz; j++) {
+        const uint32_t* Mw = M + (size_t)Nz[j] * n;
+        if (Mw[c] & Li[j] & ~Mw[k]) return false;
+    }
+    return true;
+}
+
+// Evaluates child i of the node record `nd` (one tree node).  Counts and
+// hashes the biclique when maximal; materialises the child record when it
+// has candidates.  Warp-collective.
+//
+// The child's Q part is ordered by |N(v) n L_i| descending and reduced:
+// a Q row contained in one of the first kKeepWindow kept rows is dropped,
+// since whatever it covers in the subtree the containing row covers too.
+// Large rows first make the first covering row of a non-maximal
+// descendant appear within the first few candidates.
+__device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, WarpCtx& wc,
+                               ResultAcc& acc_out, bool replay) {
+    // a replayed evaluation re-derives a donated node: its counts belong to
+    // the donor and are discarded
+    ResultAcc scratch_acc{0, 0, 0, 0};
+    ResultAcc& acc = replay ? scratch_acc : acc_out;
+    const unsigned lane = lane_id();
+    const NodeHdr* h = (const NodeHdr*)nd;
+    const uint32_t W = h->W, n = h->n, nq = h->nq;
+    const uint32_t* wmap = nd + kHdrWords;
+    const uint32_t* Lm = wmap + pad4(W);
+    const uint32_t* cand = Lm + pad4(W);
+    const uint32_t* cntv = cand + pad4(n);
+    const uint32_t* M = cntv + pad4(n);
+    const uint32_t xi = nq + i;
+    const uint32_t li = cntv[xi];
+    uint32_t* Li = W <= kSmemW ? wc.sLi : wc.scrLi;
+    uint32_t* Nz = W <= kSmemW ? wc.sNz : wc.scrNz;
+    ChildOut out{nullptr, 0, 0};
+
+    // 1. L_i = L n N(x_i), keeping only non-zero words
+    uint32_t nnz = 0;
+    for (uint32_t base = 0; base < W; base += 32) {
+        uint32_t w = base + lane;
+        uint32_t v = w < W ? (Lm[w] & M[(size_t)w * n + xi]) : 0u;
+        unsigned bal = __ballot_sync(kFull, v != 0);
+        if (v) {
+            uint32_t pos = nnz + __popc(bal & lanemask_lt());
+            Li[pos] = v;
+            Nz[pos] = w;
+        }
+        nnz += __popc(bal);
+    }
+    __syncwarp();
+    acc.nodes++;
+    acc.words += W;
+
+    // 2. maximality against Q u P[0..i); counts kept for Q'
+    const bool es = a.variant != MBE_NOES;
+    bool maximal = true;
+    for (uint32_t base = 0; base < xi; base += 32) {
+        uint32_t c = base + lane;
+        uint32_t cc = 0;
+        if (c < xi) {
+            for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+            wc.scrQcnt[c] = cc;
+        }
+        unsigned full = __ballot_sync(kFull, c < xi && cc == li);
+        acc.words += (unsigned long long)nnz * min(32u, xi - base);
+        if (full) {
+            maximal = false;
+            if (es) break;
+        }
+    }
+    __syncwarp();
+    if (!maximal) return out;
+
+    // 3. expansion over P(i..]
+    uint32_t npp = 0, nabs = 0;
+    unsigned long long sabs = 0;
+    for (uint32_t base = xi + 1; base < n; base += 32) {
+        uint32_t c = base + lane;
+        bool valid = c < n;
+        uint32_t cc = 0;
+        if (valid)
+            for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+        bool absorbed = valid && cc == li;
+        bool partial = valid && cc > 0 && cc < li;
+        if (absorbed) sabs += G.eR[cand[c]];
+        unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
+        if (partial) wc.scrKeysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
+        npp += __popc(pb);
+        nabs += __popc(ab);
+        acc.words += (unsigned long long)nnz * min(32u, n - base);
+    }
+    __syncwarp();
+    sabs = warp_sum(sabs);
+    const uint32_t nR2 = h->nRset + 1 + nabs;
+    const unsigned long long sR2 = h->sR + G.eR[cand[xi]] + sabs;
+
+    // 4. count + canonical hash
+    if (li >= a.minL && nR2 >= a.minR) {
+        const uint32_t* L0 = G.r_adj + G.r_ptr[h->root];
+        unsigned long long sl = 0;
+        for (uint32_t k = lane; k < nnz; k += 32) {
+            uint32_t bits = Li[k], b0 = wmap[Nz[k]] * 32;
+            while (bits) {
+                uint32_t t = __ffs(bits) - 1;
+                bits &= bits - 1;
+                sl += G.eL[L0[b0 + t]];
+            }
+        }
+        sl = warp_sum(sl);
+        acc.count++;
+        acc.hash += side_hash(G, sl, li, sR2, nR2);
+    }
+
+    // 5. child record
+    if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
+
+    // 5a. Q' = Q u P[0..i) restricted to rows meeting L_i, by count descending
+    uint32_t m = 0;
+    for (uint32_t base = 0; base < xi; base += 32) {
+        uint32_t c = base + lane;
+        uint32_t cc = c < xi ? wc.scrQcnt[c] : 0u;
+        unsigned bal = __ballot_sync(kFull, cc > 0);
+        if (cc > 0) wc.scrKeysQ[m + __popc(bal & lanemask_lt())] = ((unsigned long long)(0xFFFFFFFFu - cc) << 32) | c;
+        m += __popc(bal);
+    }
+    __syncwarp();
+    if (m <= 32) {
+        unsigned long long k = lane < m ? wc.scrKeysQ[lane] : kInvalidKey;
+        k = warp_sort_reg(k);
+        if (lane < m) wc.scrKeysQ[lane] = k;
+    } else {
+        uint32_t N = next_pow2(m);
+        for (uint32_t t = m + lane; t < N; t += 32) wc.scrKeysQ[t] = kInvalidKey;
+        __syncwarp();
+        warp_sort_u64(wc.scrKeysQ, N);
+    }
+    __syncwarp();
+    // 5b. reduction: greedy prefix until kKeepWindow rows are kept, then every
+    // remaining row is tested against those rows in parallel
+    uint32_t kept_c = 0, nk = 0, pos = 0;  // lane j holds the j-th kept candidate
+    while (pos < m && nk < kKeepWindow) {
+        uint32_t c = (uint32_t)wc.scrKeysQ[pos];
+        bool dom = lane < nk && row_subset(M, n, Nz, Li, nnz, c, kept_c);
+        if (!__any_sync(kFull, dom)) {
+            if (lane == nk) kept_c = c;
+            if (lane == 0) wc.scrKeysQ[nk] = c;  // compacted in place (nk <= pos)
+            nk++;
+        }
+        pos++;
+    }
+    uint32_t nq2 = nk;
+    for (uint32_t base = pos; base < m; base += 32) {
+        uint32_t idx = base + lane;
+        uint32_t c = idx < m ? (uint32_t)wc.scrKeysQ[idx] : 0u;
+        bool keep = idx < m;
+        for (uint32_t j = 0; j < nk; j++) {
+            uint32_t kc = __shfl_sync(kFull, kept_c, j);
+            if (keep && row_subset(M, n, Nz, Li, nnz, c, kc)) keep = false;
+        }
+        unsigned bal = __ballot_sync(kFull, keep);
+        __syncwarp();  // all reads of this chunk precede the compacting writes
+        if (keep) wc.scrKeysQ[nq2 + __popc(bal & lanemask_lt())] = c;
+        nq2 += __popc(bal);
+        __syncwarp();
+    }
+    acc.words += (unsigned long long)m * nnz;
+    // 5c. P' by (count ascending, parent order)
+    if (npp <= 32) {
+        unsigned long long k = lane < npp ? wc.scrKeysP[lane] : kInvalidKey;
+        k = warp_sort_reg(k);
+        if (lane < npp) wc.scrKeysP[lane] = k;
+    } else {
+        uint32_t N = next_pow2(npp);
+        for (uint32_t t = npp + lane; t < N; t += 32) wc.scrKeysP[t] = kInvalidKey;
+        __syncwarp();
+        warp_sort_u64(wc.scrKeysP, N);
+    }
+    __syncwarp();
+
+    // 5d. allocate and write the record
+    const uint32_t n2 = nq2 + npp, W2 = nnz;
+    const uint64_t rw = record_words(W2, n2);
+    uint32_t* rec;
+    if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
+        rec = wc.arena + wc.arena_top;
+        out.size = (uint32_t)rw;
+    } else {
+        unsigned long long off = 0;
+        if (lane == 0) {
+            off = pool_alloc(a, rw);
+            if (off == ~0ull) set_error(a, kErrPool, rw);
+        }
+        off = __shfl_sync(kFull, off, 0);
+        if (off == ~0ull) return out;
+        rec = a.pool + off;
+        out.size = 0;
+    }
+    uint32_t* wmap2 = rec + kHdrWords;
+    uint32_t* Lm2 = wmap2 + pad4(W2);
+    uint32_t* cand2 = Lm2 + pad4(W2);
+    uint32_t* cnt2 = cand2 + pad4(n2);
+    uint32_t* M2 = cnt2 + pad4(n2);
+    if (lane == 0) {
+        NodeHdr* h2 = (NodeHdr*)rec;
+        h2->graph = h->graph;
+        h2->root = h->root;
+        h2->W = W2;
+        h2->n = n2;
+        h2->nq = nq2;
+        h2->l = li;
+        h2->nRset = nR2;
+        h2->depth = h->depth + 1;
+        h2->sR = sR2;
+        h2->words = (uint32_t)rw;
+        h2->rlist = 0;
+    }
+    for (uint32_t k = lane; k < W2; k += 32) {
+        wmap2[k] = wmap[Nz[k]];
+        Lm2[k] = Li[k];
+    }
+    for (uint32_t t = lane; t < nq2; t += 32) {
+        uint32_t c = (uint32_t)wc.scrKeysQ[t];
+        cand2[t] = cand[c];
+        cnt2[t] = 0;
+        for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + t] = M[(size_t)Nz[k] * n + c] & Li[k];
+    }
+    for (uint32_t t = lane; t < npp; t += 32) {
+        unsigned long long key = wc.scrKeysP[t];
+        uint32_t c = nq + (uint32_t)key;
+        uint32_t pos2 = nq2 + t;
+        cand2[pos2] = cand[c];
+        cnt2[pos2] = (uint32_t)(key >> 32);
+        for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + pos2] = M[(size_t)Nz[k] * n + c] & Li[k];
+    }
+    acc.words += (unsigned long long)W2 * n2;
+    __syncwarp();
+    out.rec = rec;
+    out.nchild = npp;
+    return out;
+}
+
+// Gives the upper half of the remaining children of the shallowest frame
+// with at least donate_min of them to a waiting warp.  A frame whose record
+// is in the node pool is shared by pointer; a frame whose record lives in
+// this warp's arena is described by the child-index path from frame 0
+// (always a pool record), which the receiver replays.  Warp-collective.
+__device__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc) {
+    unsigned lane = lane_id();
+    int k = -1;
+    for (int base = 0; base <= depth && k < 0; base += 32) {
+        int f = base + (int)lane;
+        bool ok = false;
+        if (f <= depth) {
+            Frame fr = frames[f];
+            uint32_t* nd = (uint32_t*)fr.node;
+            bool in_arena = nd >= wc.arena && nd < wc.arena + a.arena_words;
+            ok = fr.end > fr.next && fr.end - fr.next >= a.donate_min && (!in_arena || f <= (int)kMaxPath);
+        }
+        unsigned bal = __ballot_sync(kFull, ok);
+        if (bal) k = base + __ffs(bal) - 1;
+    }
+    if (k < 0) return;
+    Frame fr = frames[k];
+    uint32_t rem = fr.end - fr.next;
+    uint32_t give = rem / 2;
+    if (give == 0) return;
+    uint32_t mid = fr.end - give;
+    uint32_t* nd = (uint32_t*)fr.node;
+    bool in_arena = nd >= wc.arena && nd < wc.arena + a.arena_words;
+    // path element j = the child of frame j that frame j+1 expands (k <= kMaxPath <= 31)
+    uint32_t pe = ((int)lane < k) ? frames[lane].next - 1 : 0u;
+    Task t{};
+    t.begin = mid;
+    t.end = fr.end;
+    t.node = in_arena ? frames[0].node : fr.node;
+    t.plen = in_arena ? (uint32_t)k : 0u;
+    for (int j = 0; j < (int)t.plen; j++) t.path[j] = __shfl_sync(kFull, pe, j);
+    if (lane == 0) {
+        frames[k].end = mid;
+        push_task(a, t);
+    }
+    __syncwarp();
+}
+
+__device__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
+    if (lane_id() == 0) {
+        ResultAcc* r = &a.results[graph];
+        if (acc.count) atomicAdd(&r->count, acc.count);
+        if (acc.hash) atomicAdd(&r->hash, acc.hash);
+        if (acc.nodes) atomicAdd(&r->nodes, acc.nodes);
+        if (acc.words) atomicAdd(&r->words, acc.words);
+    }
+    acc = ResultAcc{0, 0, 0, 0};
+}
+
+__global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
+    __shared__ uint32_t sLi[kWarpsB][kSmemW];
+    __shared__ uint32_t sNz[kWarpsB][kSmemW];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const size_t gw = (size_t)blockIdx.x * kWarpsB + warp;
+    Frame* frames = a.frames + gw * a.max_frames;
+    WarpCtx wc;
+    wc.arena = a.arena + gw * a.arena_words;
+    wc.arena_top = 0;
+    uint32_t* scr = a.scratch + gw * a.scratch_words;
+    // scratch: Li[max_W] Nz[max_W] qcnt[scr_n] | keysP[kc] keysQ[kc] (u64, kc = pow2 >= scr_n)
+    wc.scrLi = scr;
+    wc.scrNz = scr + a.max_W;
+    wc.scrQcnt = scr + 2 * (size_t)a.max_W;
+    size_t koff = (2 * (size_t)a.max_W + a.scr_n + 1) & ~(size_t)1;
+    wc.scrKeysP = (unsigned long long*)(scr + koff);
+    wc.scrKeysQ = wc.scrKeysP + a.scr_kc;
+    wc.sLi = sLi[warp];
+    wc.sNz = sNz[warp];
+    const bool donate = a.variant != MBE_NOWS;
+    ResultAcc acc{0, 0, 0, 0};
+    uint32_t evals = 0;
+    Task t{};
+    uint32_t my_path = 0;
+    while (pop_task(a, t, my_path)) {
+        const uint32_t graph = ((const NodeHdr*)t.node)->graph;
+        const GraphView G = a.graphs[graph];
+        wc.arena_top = 0;
+        int depth = 0;
+        {
+            uint32_t p0 = __shfl_sync(kFull, my_path, 0);
+            if (lane == 0) {
+                Frame f0;
+                f0.node = t.node;
+                f0.next = t.plen ? p0 + 1 : t.begin;
+                f0.end = t.plen ? p0 + 1 : t.end;
+                f0.arena_mark = 0;
+                f0.pad = 0;
+                frames[0] = f0;
+            }
+        }
+        __syncwarp();
+        // re-derive the donated node along its path (uncounted)
+        bool replay_ok = true;
+        for (uint32_t j = 0; j < t.plen; j++) {
+            uint32_t idx = __shfl_sync(kFull, my_path, j);
+            uint32_t nxt = __shfl_sync(kFull, my_path, (j + 1) & 31);
+            uint32_t mark = wc.arena_top;
+            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, wc, acc, true);
+            if (!co.rec) {
+                if (lane == 0) set_error(a, kErrReplay, j);
+                replay_ok = false;
+                break;
+            }
+            wc.arena_top += co.size;
+            depth = (int)j + 1;
+            if (lane == 0) {
+                Frame nf;
+                nf.node = (unsigned long long)co.rec;
+                bool last = j + 1 == t.plen;
+                nf.next = last ? t.begin : nxt + 1;
+                nf.end = last ? t.end : nxt + 1;
+                nf.arena_mark = mark;
+                nf.pad = 0;
+                frames[depth] = nf;
+            }
+            __syncwarp();
+        }
+        if (!replay_ok) depth = -1;
+        while (depth >= 0) {
+            Frame f = frames[depth];
+            if (f.next >= f.end) {
+                wc.arena_top = f.arena_mark;
+                depth--;
+                continue;
+            }
+            if (donate && (evals & 3u) == 0) {
+                // waiting warps = tickets taken beyond the tasks pushed
+                uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
+                if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) try_donate(a, frames, depth, wc);
+                f = frames[depth];
+                if (f.next >= f.end) continue;
+            }
+            if (lane == 0) frames[depth].next = f.next + 1;
+            __syncwarp();
+            uint32_t mark = wc.arena_top;
+            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, f.next, wc, acc, false);
+            evals++;
+            if ((evals & 1023u) == 0 && lane == 0) atomicAdd(a.progress, 1ull);
+            if (co.rec) {
+                if (depth + 1 >= (int)a.max_frames) {
+                    if (lane == 0) set_error(a, kErrFrames, depth);
+                    break;
+                }
+                wc.arena_top += co.size;
+                depth++;
+                if (lane == 0) {
+                    Frame nf;
+                    nf.node = (unsigned long long)co.rec;
+                    nf.next = 0;
+                    nf.end = co.nchild;
+                    nf.arena_mark = mark;
+                    nf.pad = 0;
+                    frames[depth] = nf;
+                }
+                __syncwarp();
+            }
+            if (ld_volatile(a.error)) break;
+        }
+        flush_acc(a, graph, acc);
+        if (lane == 0) {
+            __threadfence();
+            atomicSub(a.pending, 1);
+            atomicAdd(a.progress, 1ull);
+        }
+        __syncwarp();
+    }
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host driver
+
+void EngineBuffers::release() {
+    for (DevBuf* b : {&graphs, &roots, &ctrl, &tasks, &ready, &cmap, &a_cl, &a_cnt, &a_keys, &pool, &arena, &frames,
+                      &scratch, &results, &retry_in, &retry_list})
+        b->free();
+}
+
+mbe_status DevBuf::ensure(size_t need) {
+    if (need <= bytes) return MBE_OK;
+    free();
+    size_t want = std::max(need, (size_t)256);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        cudaGetLastError();
+        return fail(MBE_ERR_OUT_OF_MEMORY, "device allocation of " + std::to_string(want) + " bytes failed");
+    }
+    bytes = want;
+    return MBE_OK;
+}
+
+void DevBuf::free() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+// Control block layout (words): see offsets below.
+namespace {
+struct Ctrl {
+    unsigned long long pool_top;
+    unsigned long long progress;
+    unsigned long long error_info;
+    uint32_t root_next;
+    uint32_t n_retry;
+    uint32_t q_tail;
+    uint32_t q_head;
+    int pending;
+    uint32_t q_done;
+    int error;
+    uint32_t max_n;
+    uint32_t pad[2];
+};
+}  // namespace
+
+mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
+                      const std::vector<const DeviceGraph*>& gs, const std::vector<uint2>& roots,
+                      std::vector<ResultAcc>& results, EngineStats* stats) {
+    const uint32_t ng = (uint32_t)gs.size();
+    results.assign(ng, ResultAcc{0, 0, 0, 0});
+    if (ng == 0 || roots.empty()) return MBE_OK;
+    uint32_t maxNR = 1, maxW = 1;
+    for (const DeviceGraph* g : gs) {
+        maxNR = std::max(maxNR, g->nR);
+        maxW = std::max(maxW, (g->max_rdeg + 31) / 32);
+    }
+    const uint32_t keys_cap = (uint32_t)std::max<size_t>(2048, [&] {
+        size_t p = 1;
+        while (p < maxNR) p <<= 1;
+        return p;
+    }());
+    int dev = 0;
+    MBE_CUDA_TRY(cudaGetDevice(&dev));
+    int n_sm = 0;
+    MBE_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    int occA = 0, occB = 0;
+    MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, expand_roots_kernel, kThreadsA, 0));
+    MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occB, dfs_kernel, kThreadsB, 0));
+    uint32_t gridA = (uint32_t)n_sm * (uint32_t)std::max(1, std::min(occA, 2));
+    uint32_t bpsm = cfg.blocks_per_sm ? cfg.blocks_per_sm : (uint32_t)std::max(1, occB);
+    bpsm = std::min<uint32_t>(bpsm, (uint32_t)std::max(1, occB));
+    uint32_t gridB = (uint32_t)n_sm * bpsm;
+    uint32_t nwarpsB = gridB * kWarpsB;
+    const uint32_t q_margin = nwarpsB + 1024;
+    const uint32_t task_cap = (uint32_t)std::min<size_t>(roots.size() + q_margin + (size_t)cfg.extra_tasks, 0x7FFFFFFF);
+    const uint32_t max_frames = cfg.max_frames;
+    // Arena and node pool are sized once per context from free device
+    // memory: per-warp DFS arenas take ~30% of it (at most 16 MiB each), the
+    // shared node pool ~15% (at most 32 GiB).
+    if (!eb.arena_words || !eb.pool_words) {
+        size_t fr = 0, tot = 0;
+        MBE_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+        uint64_t per_warp = (uint64_t)(fr * 0.30) / nwarpsB / 4;
+        eb.arena_words = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(per_warp, 1u << 16), 1u << 22) & ~31u;
+        uint64_t pool = (uint64_t)(fr * 0.15) / 4;
+        eb.pool_words = std::min<uint64_t>(std::max<uint64_t>(pool, 1ull << 26), 1ull << 33) & ~31ull;
+    }
+    const uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
+    const uint64_t pool_words = cfg.pool_words ? std::min<uint64_t>(cfg.pool_words, eb.pool_words) : eb.pool_words;
+    const uint32_t retry_cap = 1u << 16;
+
+    mbe_status st;
+    std::vector<GraphView> views;
+    for (const DeviceGraph* g : gs) views.push_back(view_of(*g));
+    if ((st = eb.graphs.ensure(sizeof(GraphView) * ng))) return st;
+    if ((st = eb.roots.ensure(sizeof(uint2) * roots.size()))) return st;
+    if ((st = eb.ctrl.ensure(sizeof(Ctrl)))) return st;
+    if ((st = eb.tasks.ensure(sizeof(Task) * (size_t)task_cap))) return st;
+    if ((st = eb.ready.ensure(sizeof(uint32_t) * (size_t)task_cap))) return st;
+    size_t cmap_bytes = sizeof(int) * (size_t)gridA * maxNR;
+    if ((st = eb.cmap.ensure(cmap_bytes))) return st;
+    if ((st = eb.a_cl.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
+    if ((st = eb.a_cnt.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
+    if ((st = eb.a_keys.ensure(sizeof(unsigned long long) * (size_t)gridA * keys_cap))) return st;
+    if ((st = eb.pool.ensure(sizeof(uint32_t) * eb.pool_words))) return st;
+    if ((st = eb.arena.ensure(sizeof(uint32_t) * (size_t)nwarpsB * eb.arena_words))) return st;
+    if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * max_frames))) return st;
+    if ((st = eb.results.ensure(sizeof(ResultAcc) * ng))) return st;
+    if ((st = eb.retry_in.ensure(sizeof(uint32_t) * (size_t)retry_cap))) return st;
+    // cmap must be all -1 at kernel entry; kernels restore it after each root
+    MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));
+    MBE_CUDA_TRY(cudaMemcpyAsync(eb.graphs.ptr, views.data(), sizeof(GraphView) * ng, cudaMemcpyHostToDevice, s));
+    MBE_CUDA_TRY(cudaMemcpyAsync(eb.roots.ptr, roots.data(), sizeof(uint2) * roots.size(), cudaMemcpyHostToDevice, s));
+    MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
+
+    Ctrl* ctrl = (Ctrl*)eb.ctrl.ptr;
+    EngineArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.graphs = (const GraphView*)eb.graphs.ptr;
+    a.n_graphs = ng;
+    a.variant = cfg.variant;
+    a.minL = cfg.minL;
+    a.minR = cfg.minR;
+    a.donate_min = std::max(2u, cfg.donate_min);
+    a.roots = (const uint2*)eb.roots.ptr;
+    a.n_roots = (uint32_t)roots.size();
+    a.root_next = &ctrl->root_next;
+    a.retry = (uint32_t*)eb.retry_in.ptr;
+    a.n_retry = &ctrl->n_retry;
+    a.retry_cap = retry_cap;
+    a.pool = (uint32_t*)eb.pool.ptr;
+    a.pool_words = pool_words;
+    a.pool_top = &ctrl->pool_top;
+    a.pool_watermark = pool_words / 2;
+    a.tasks = (Task*)eb.tasks.ptr;
+    a.ready = (uint32_t*)eb.ready.ptr;
+    a.task_cap = task_cap;
+    a.q_tail = &ctrl->q_tail;
+    a.q_head = &ctrl->q_head;
+    a.q_done = &ctrl->q_done;
+    a.q_margin = q_margin;
+    a.pending = &ctrl->pending;
+    a.progress = &ctrl->progress;
+    a.cmap = (int*)eb.cmap.ptr;
+    a.a_cl = (uint32_t*)eb.a_cl.ptr;
+    a.a_cnt = (uint32_t*)eb.a_cnt.ptr;
+    a.a_keys = (unsigned long long*)eb.a_keys.ptr;
+    a.maxNR = maxNR;
+    a.keys_cap = keys_cap;
+    a.arena = (uint32_t*)eb.arena.ptr;
+    a.arena_words = arena_words;
+    a.frames = (Frame*)eb.frames.ptr;
+    a.max_frames = max_frames;
+    a.max_n = &ctrl->max_n;
+    a.max_W = maxW;
+    a.results = (ResultAcc*)eb.results.ptr;
+    a.error = &ctrl->error;
+    a.error_info = &ctrl->error_info;
+    a.timeout_ns = cfg.timeout_ns;
+
+    // Roots that did not fit the pool in one chunk are retried first in the
+    // next chunk (from a host copy), then the main list resumes.
+    std::vector<uint2> pending_roots;  // retry roots carried to the next chunk
+    uint32_t main_next = 0;
+    cudaEvent_t e0, e1, e2;
+    MBE_CUDA_TRY(cudaEventCreate(&e0));
+    MBE_CUDA_TRY(cudaEventCreate(&e1));
+    MBE_CUDA_TRY(cudaEventCreate(&e2));
+    float ms_a = 0, ms_b = 0;
+    uint32_t chunks = 0;
+    mbe_status result = MBE_OK;
+    while (result == MBE_OK && (main_next < roots.size() || !pending_roots.empty())) {
+        chunks++;
+        // Chunk root list: retried roots, then the main list from main_next.
+        const uint2* list;
+        uint32_t list_n;
+        std::vector<uint2> chunk_list;
+        if (!pending_roots.empty()) {
+            chunk_list = pending_roots;
+            list_n = (uint32_t)chunk_list.size();
+            if ((st = eb.retry_list.ensure(sizeof(uint2) * list_n))) return st;
+            MBE_CUDA_TRY(cudaMemcpyAsync(eb.retry_list.ptr, chunk_list.data(), sizeof(uint2) * list_n,
+                                         cudaMemcpyHostToDevice, s));
+            list = (const uint2*)eb.retry_list.ptr;
+        } else {
+            list = (const uint2*)eb.roots.ptr + main_next;
+            list_n = (uint32_t)roots.size() - main_next;
+        }
+        a.roots = list;
+        a.n_roots = list_n;
+        MBE_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
+        MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
+        MBE_CUDA_TRY(cudaEventRecord(e0, s));
+        expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
+        MBE_CUDA_TRY(cudaGetLastError());
+        MBE_CUDA_TRY(cudaEventRecord(e1, s));
+        // DFS scratch is laid out for the largest record this chunk made
+        uint32_t max_n = 0;
+        MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
+        MBE_CUDA_TRY(cudaStreamSynchronize(s));
+        {
+            uint32_t scr_n = std::max<uint32_t>(max_n, 32);
+            size_t kc = 32;
+            while (kc < scr_n) kc <<= 1;
+            size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc, 32);
+            if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
+            a.scratch = (uint32_t*)eb.scratch.ptr;
+            a.scratch_words = (uint32_t)sw;
+            a.scr_n = scr_n;
+            a.scr_kc = (uint32_t)kc;
+        }
+        dfs_kernel<<<gridB, kThreadsB, 0, s>>>(a);
+        MBE_CUDA_TRY(cudaGetLastError());
+        MBE_CUDA_TRY(cudaEventRecord(e2, s));
+        Ctrl hc;
+        MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+        MBE_CUDA_TRY(cudaStreamSynchronize(s));
+        float t1 = 0, t2 = 0;
+        cudaEventElapsedTime(&t1, e0, e1);
+        cudaEventElapsedTime(&t2, e1, e2);
+        ms_a += t1;
+        ms_b += t2;
+        if (hc.error) {
+            static const char* names[] = {"none", "node pool exhausted", "task queue full", "device wait timed out",
+                                          "search deeper than the frame stack", "scratch too small"};
+            mbe_status code = hc.error == kErrTimeout ? MBE_ERR_DEVICE_TIMEOUT
+                              : hc.error == kErrPool  ? MBE_ERR_OUT_OF_MEMORY
+                                                      : MBE_ERR_CAPACITY;
+            result = fail(code, std::string("enumeration kernel: ") + names[hc.error < 6 ? hc.error : 0] +
+                                    " (info " + std::to_string(hc.error_info) + ")");
+            break;
+        }
+        uint32_t consumed = std::min(hc.root_next, list_n);
+        std::vector<uint32_t> retry_idx(std::min(hc.n_retry, retry_cap));
+        if (!retry_idx.empty())
+            MBE_CUDA_TRY(cudaMemcpy(retry_idx.data(), a.retry, sizeof(uint32_t) * retry_idx.size(),
+                                    cudaMemcpyDeviceToHost));
+        if (hc.n_retry > retry_cap || consumed == 0 || consumed == (uint32_t)retry_idx.size()) {
+            // nothing fitted an empty pool: more chunks would not help
+            result = fail(MBE_ERR_OUT_OF_MEMORY, "a root's search record does not fit the node pool");
+            break;
+        }
+        std::vector<uint2> next_pending;
+        const uint2* host_list = pending_roots.empty() ? roots.data() + main_next : chunk_list.data();
+        for (uint32_t r : retry_idx) next_pending.push_back(host_list[r]);
+        if (!pending_roots.empty()) {
+            for (uint32_t r = consumed; r < list_n; r++) next_pending.push_back(chunk_list[r]);
+        } else {
+            main_next += consumed;
+        }
+        pending_roots.swap(next_pending);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (result != MBE_OK) return result;
+    MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
+    if (stats) {
+        stats->ms_expand = ms_a;
+        stats->ms_dfs = ms_b;
+        stats->chunks = chunks;
+        stats->grid_a = gridA;
+        stats->grid_b = gridB;
+    }
+    return MBE_OK;
+}
+
+}  // namespace mbe

@@ -1,0 +1,146 @@
+// Enumeration engine: device data structures shared by the root-expansion
+// kernel, the DFS kernel and the host driver.
+//
+// Search semantics (same result set as src/mbe_cuMBE.cuh):
+//   root x (a rank of the R side):  L0 = N(x); candidates C = N(N(x)) \ {x};
+//     Q0 = candidates of lower rank (processed before x), P0 = higher rank.
+//     The root is non-maximal iff some v in Q0 is adjacent to all of L0.
+//   node (L, R, P, Q), children x_i = P[i] in order:
+//     L_i = L n N(x_i); non-maximal iff some v in Q u P[0..i) covers L_i;
+//     absorbed  = {v in P(i..] : N(v) covers L_i}  -> R_i;
+//     P_i       = {v in P(i..] : 0 < |N(v) n L_i| < |L_i|}, stably sorted by
+//                 that count (the reference's min-count pivot order);
+//     Q_i       = {v in Q u P[0..i) : |N(v) n L_i| > 0}.
+//
+// Every internal node is a self-contained RECORD: its L is a set of bit
+// positions of the root universe (bit j <-> L0[j]); each candidate holds a
+// bit row over the node's words; rows are stored word-major so that a warp
+// reading 32 consecutive candidates of one word issues one 128-byte load.
+// A child record keeps only the words where L_i is non-zero, with rows
+// pre-masked by L_i.
+#pragma once
+#include <stdint.h>
+
+#include "graph_dev.cuh"
+
+namespace mbe {
+
+constexpr uint32_t kHdrWords = 16;
+constexpr uint32_t kMaxPath = 27;
+
+__host__ __device__ inline uint32_t pad4(uint32_t x) { return (x + 3u) & ~3u; }
+
+// record layout (32-bit words):
+//   [0,16)      header
+//   wmap[W]     root word index of each word
+//   Lm[W]       L as bits per word
+//   cand[n]     candidate ranks; [0,nq) = Q part, [nq,n) = P part
+//   cnt[n]      |N(v) n L| (P part)
+//   M[W*n]      word-major bit rows
+struct NodeHdr {
+    uint32_t graph;
+    uint32_t root;
+    uint32_t W;
+    uint32_t n;
+    uint32_t nq;
+    uint32_t l;
+    uint32_t nRset;
+    uint32_t depth;
+    unsigned long long sR;
+    uint32_t words;
+    uint32_t rlist;   // word offset (from record start) of the R list, 0 if absent
+    uint32_t pad[4];
+};
+static_assert(sizeof(NodeHdr) == kHdrWords * 4, "header size");
+
+__host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n) {
+    return kHdrWords + 2ull * pad4(W) + 2ull * pad4(n) + (((uint64_t)W * n + 3) & ~3ull);
+}
+
+// A unit of work: children [begin, end) of the node reached from the pool
+// record `node` by following child indices path[0..plen).  The receiver
+// re-derives the nodes on the path (deterministic), so donating a node that
+// lives in the donor's private arena copies nothing.
+struct Task {
+    unsigned long long node;     // device pointer of a node-pool record
+    uint32_t begin, end;         // child range (P-part indices)
+    uint32_t plen;
+    uint32_t path[kMaxPath];
+};
+static_assert(sizeof(Task) == 128, "task size");
+
+struct Frame {
+    unsigned long long node;
+    uint32_t next, end;
+    uint32_t arena_mark;      // arena top to restore when the frame pops
+    uint32_t pad;
+};
+
+struct ResultAcc {
+    unsigned long long count, hash, nodes, words;
+};
+
+enum : int {
+    kErrNone = 0,
+    kErrPool = 1,       // node pool exhausted
+    kErrQueue = 2,      // task queue capacity
+    kErrTimeout = 3,    // a bounded wait ran out
+    kErrFrames = 4,     // DFS deeper than the frame stack
+    kErrScratch = 5,    // per-warp scratch too small
+    kErrReplay = 6,     // a donated path did not re-derive
+};
+
+struct EngineArgs {
+    const GraphView* graphs;
+    uint32_t n_graphs;
+    uint32_t variant;
+    uint32_t minL, minR;       // thresholds in L/R orientation (batched: same for all)
+    uint32_t donate_min;
+    // root list: (graph, rank) pairs, processed from index 0
+    const uint2* roots;
+    uint32_t n_roots;
+    uint32_t* root_next;       // next root index to expand
+    uint32_t* retry;           // roots whose record did not fit the pool
+    uint32_t* n_retry;
+    uint32_t retry_cap;
+    // node pool (bump allocator, reset per chunk)
+    uint32_t* pool;
+    unsigned long long pool_words;
+    unsigned long long* pool_top;
+    unsigned long long pool_watermark;
+    // task queue
+    Task* tasks;
+    uint32_t* ready;           // per slot: ticket+1 of the task stored, 0 = free
+    uint32_t task_cap;         // ring capacity
+    uint32_t* q_tail;          // tickets handed to producers
+    uint32_t* q_head;          // tickets handed to consumers
+    uint32_t* q_done;          // tasks read out of their slot
+    uint32_t q_margin;         // free slots a donor leaves untouched
+    int* pending;
+    unsigned long long* progress;
+    // phase A per-block scratch
+    int* cmap;                 // [gridA][maxNR]  vertex -> candidate slot, -1 when free
+    uint32_t* a_cl;            // [gridA][maxNR]
+    uint32_t* a_cnt;           // [gridA][maxNR]
+    unsigned long long* a_keys;// [gridA][pow2(maxNR)]
+    uint32_t maxNR;
+    uint32_t keys_cap;
+    uint32_t* max_n;           // largest candidate count of any root record
+    // phase B per-warp memory
+    uint32_t* arena;
+    uint32_t arena_words;
+    Frame* frames;
+    uint32_t max_frames;
+    uint32_t* scratch;
+    uint32_t scratch_words;
+    uint32_t scr_n;            // candidate bound the scratch is laid out for
+    uint32_t scr_kc;           // key-array capacity (power of two >= scr_n)
+    uint32_t max_W;            // largest universe word count
+    // results
+    ResultAcc* results;        // [n_graphs]
+    int* error;
+    unsigned long long* error_info;
+    unsigned long long timeout_ns;
+};
+
+}  // namespace mbe

@@ -1,0 +1,53 @@
+// Host interface of the enumeration engine (used by capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "engine.cuh"
+#include "graph_dev.cuh"
+
+namespace mbe {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    mbe_status ensure(size_t need);
+    void free();
+};
+
+// Device memory reused across calls on one context.
+struct EngineBuffers {
+    DevBuf graphs, roots, ctrl, tasks, ready, cmap, a_cl, a_cnt, a_keys, pool, arena, frames, scratch, results,
+        retry_in, retry_list;
+    // sizes chosen at first use from the device's free memory
+    uint32_t arena_words = 0;
+    uint64_t pool_words = 0;
+    void release();
+};
+
+struct EngineConfig {
+    uint32_t variant = 0;
+    uint32_t minL = 0, minR = 0;        // thresholds in L/R orientation
+    uint32_t donate_min = 2;
+    uint32_t blocks_per_sm = 0;         // 0 = occupancy limit
+    uint32_t max_frames = 512;
+    uint32_t arena_words = 0;           // per warp; 0 = sized from free memory
+    uint64_t pool_words = 0;            // node pool; 0 = sized from free memory
+    uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
+    unsigned long long timeout_ns = 60ull * 1000000000ull;
+};
+
+struct EngineStats {
+    float ms_expand = 0, ms_dfs = 0;
+    uint32_t chunks = 0, grid_a = 0, grid_b = 0;
+};
+
+// Runs root expansion + DFS for the given (graph, rank) roots.  results[g]
+// receives the accumulated count / hash / nodes / words of graph g.
+mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
+                      const std::vector<const DeviceGraph*>& graphs, const std::vector<uint2>& roots,
+                      std::vector<ResultAcc>& results, EngineStats* stats);
+
+}  // namespace mbe

@@ -1,0 +1,218 @@
+/*
+ * mbe.h - C ABI of libmbe, a GB300-native (sm_103a) maximal biclique
+ * enumeration engine that is a drop-in for the cuMBE enumeration path.
+ *
+ * The reference (NTUDDSNLab/cuMBE) has no library API: its boundary is the
+ * `mbe <graph.bi> [cuMBE|noRS|noES|noWS]` command (src/main.cu:9,121-122),
+ * the `.bi` text format it parses (src/main.cu:38-48), the orientation swap
+ * (src/main.cu:65-70), the CSR transpose kernel (src/transpose.cuh:1-52),
+ * the host root ordering (src/header.cuh:55-63) and the cooperative launch
+ * of CUDA_MBE_<variant> (src/main.cu:190-199) whose only result is the
+ * int32 count in `num_mb` (src/main.cu:207).  Each entry point below names
+ * the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every call returns an mbe_status; nothing calls exit().  A failing call
+ *    leaves a message retrievable with mbe_last_error().
+ *  - Vertex ids are uint32, CSR offsets uint64.  Orientation is the file's:
+ *    "rows" are the first header field of a `.bi` file, "cols" the second.
+ *  - A context owns one CUDA stream on one device.  Calls on different
+ *    contexts may run from different host threads; calls on one context
+ *    must not overlap.
+ *  - Counts are uint64 (the reference counts in int32 and wraps past 2^31).
+ */
+#ifndef MBE_H_
+#define MBE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MBE_API __attribute__((visibility("default")))
+#else
+#define MBE_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mbe_status {
+    MBE_OK = 0,
+    MBE_ERR_INVALID_ARG = 1,
+    MBE_ERR_IO = 2,
+    MBE_ERR_FORMAT = 3,          /* malformed .bi text or CSR arrays        */
+    MBE_ERR_CUDA = 4,            /* a CUDA runtime call failed              */
+    MBE_ERR_OUT_OF_MEMORY = 5,   /* device pool / arena exhausted           */
+    MBE_ERR_DEVICE_TIMEOUT = 6,  /* a bounded device-side wait ran out      */
+    MBE_ERR_CAPACITY = 7,        /* a fixed-size device structure overflowed */
+    MBE_ERR_NO_DEVICE = 8,       /* no CUDA device / driver available       */
+    MBE_ERR_BUSY = 9             /* server: admission queue full            */
+} mbe_status;
+
+/* The four algorithm names the reference's CLI accepts
+ * (src/header.cuh:12, src/main.cu:121-122).  All four return the same
+ * count and hash; they differ in how the engine counts and schedules:
+ *   MBE_CUMBE  reverse scanning (L-side scatter) + early stop + stealing
+ *   MBE_NORS   candidate-side (forward) counting in the root expansion
+ *   MBE_NOES   no early exit in the maximality and count loops
+ *   MBE_NOWS   no work donation between warps (static root ownership)   */
+typedef enum mbe_variant {
+    MBE_CUMBE = 0,
+    MBE_NORS = 1,
+    MBE_NOES = 2,
+    MBE_NOWS = 3
+} mbe_variant;
+
+typedef struct mbe_graph mbe_graph;
+typedef struct mbe_ctx mbe_ctx;
+
+typedef struct mbe_graph_info {
+    uint32_t n_rows;
+    uint32_t n_cols;
+    uint64_t n_edges;
+    uint32_t max_row_deg;
+    uint32_t max_col_deg;
+    uint32_t n_dup_dropped;      /* duplicate entries removed on ingest    */
+    uint32_t swapped;            /* 1 when rows > cols: rows become the
+                                    L side (src/main.cu:65-70)             */
+} mbe_graph_info;
+
+/* Synthetic bipartite Chung-Lu generator (replaces the reference's
+ * KONECT download + data/gen_bi.cpp conversion, which needs network).
+ * Weights w_i = (i+1)^(-1/(gamma-1)) per side, scaled to n_edges and capped
+ * at max_deg; endpoints drawn with a splitmix64 stream seeded by `seed`;
+ * duplicates rejected until n_edges distinct edges exist (or 64*n_edges
+ * draws were made).  `planted` adds near-bicliques K_{planted_rows,
+ * planted_cols} at edge density planted_density, half of each side drawn
+ * from the 1% highest-weight vertices (hubs) and half uniformly.
+ * gamma <= 0 on a side selects uniform endpoints (Erdos-Renyi G(n,m)). */
+typedef struct mbe_gen_params {
+    uint32_t n_rows;
+    uint32_t n_cols;
+    uint64_t n_edges;
+    double gamma_rows;
+    double gamma_cols;
+    uint32_t max_deg;            /* 0 = uncapped                           */
+    uint64_t seed;
+    uint32_t planted;            /* number of planted blocks               */
+    uint32_t planted_rows;
+    uint32_t planted_cols;
+    double planted_density;
+} mbe_gen_params;
+
+/* Enumeration options. */
+enum {
+    MBE_OPT_NO_HASH = 1u << 0,   /* skip the per-biclique canonical hash    */
+    MBE_OPT_EMIT = 1u << 1,      /* materialise bicliques into emit buffers */
+    MBE_OPT_TIMING = 1u << 2     /* fill mbe_result.ms with device time     */
+};
+
+typedef struct mbe_opts {
+    uint32_t flags;
+    uint32_t min_rows;           /* thresholded enumeration: |A| >= min_rows */
+    uint32_t min_cols;           /*                          |B| >= min_cols */
+    /* tuning (0 = engine default / autotuned) */
+    uint32_t warps_per_block;
+    uint32_t blocks_per_sm;
+    uint32_t donate_min;         /* min remaining children to donate       */
+    uint32_t stack_words;        /* per-warp DFS arena size, 32-bit words  */
+    /* optional output stream (MBE_OPT_EMIT): host buffers, see mbe_emit_* */
+    uint32_t* emit_offsets;      /* [emit_cap_bicliques+1] into emit_ids    */
+    uint32_t* emit_ids;          /* rows of a biclique, then its cols       */
+    uint32_t* emit_nrows;        /* [emit_cap_bicliques] |A| per biclique   */
+    uint64_t emit_cap_bicliques;
+    uint64_t emit_cap_ids;
+} mbe_opts;
+
+typedef struct mbe_result {
+    uint64_t count;              /* maximal bicliques (thresholds applied)  */
+    uint64_t hash;               /* sum over bicliques of mbe_biclique_hash */
+    uint64_t nodes;              /* search-tree nodes evaluated             */
+    uint64_t words;              /* 32-bit words of set data streamed       */
+    uint64_t emitted;            /* bicliques written to emit buffers       */
+    float ms;                    /* device time of the enumeration kernels  */
+    float ms_prep;               /* device time of the root expansion       */
+} mbe_result;
+
+/* ---- graphs (host side; no device needed) ------------------------------ */
+
+/* Parses a `.bi` file: header "R L E", R lines "start length", E lines
+ * "nbr x" with the second token ignored (src/main.cu:38-48).  Row lists
+ * are sorted and deduplicated (the reference's own files hold unsorted
+ * lists, data/gen_bi.cpp:78).  Replaces the ifstream reader at
+ * src/main.cu:38-48. */
+MBE_API mbe_status mbe_graph_load_bi(const char* path, mbe_graph** out);
+
+/* Builds a graph from a host CSR in file orientation.  Lists may be
+ * unsorted and hold duplicates; both are normalised on ingest.  Replaces
+ * the managed-memory CSR of src/main.cu:41-47. */
+MBE_API mbe_status mbe_graph_from_csr(uint32_t n_rows, uint32_t n_cols,
+                              const uint64_t* row_ptr, const uint32_t* col_idx,
+                              mbe_graph** out);
+
+MBE_API mbe_status mbe_graph_generate(const mbe_gen_params* params, mbe_graph** out);
+
+/* Writes the `.bi` layout data/gen_bi.cpp:72-79 writes. */
+MBE_API mbe_status mbe_graph_write_bi(const mbe_graph* g, const char* path);
+
+MBE_API mbe_status mbe_graph_info_get(const mbe_graph* g, mbe_graph_info* out);
+
+/* Copies the normalised CSR out: row_ptr[n_rows+1], col_idx[n_edges]. */
+MBE_API mbe_status mbe_graph_copy_csr(const mbe_graph* g, uint64_t* row_ptr,
+                              uint32_t* col_idx);
+
+MBE_API void mbe_graph_free(mbe_graph* g);
+
+/* ---- contexts ------------------------------------------------------------ */
+
+MBE_API mbe_status mbe_ctx_create(int device, mbe_ctx** out);
+MBE_API void mbe_ctx_destroy(mbe_ctx* ctx);
+
+/* Message of the last failing call on this host thread. */
+MBE_API const char* mbe_last_error(void);
+
+/* ---- device-resident graph -------------------------------------------- */
+
+/* Copies the graph to the device, builds the transposed CSR with the
+ * transpose kernels (replaces CUDA_TRANSPOSE, src/transpose.cuh:1-52) and
+ * the root order (replaces my_memset_sort, src/header.cuh:55-63).  The
+ * device copy stays resident in the context until mbe_graph_release or
+ * mbe_ctx_destroy; repeated calls with the same graph are no-ops. */
+MBE_API mbe_status mbe_graph_upload(mbe_ctx* ctx, const mbe_graph* g);
+MBE_API mbe_status mbe_graph_release(mbe_ctx* ctx, const mbe_graph* g);
+
+/* ---- enumeration -------------------------------------------------------- */
+
+/* Counts (and hashes, and optionally emits) the maximal bicliques of g.
+ * Replaces the cooperative launch of CUDA_MBE_<variant>
+ * (src/main.cu:190-207, src/mbe_cuMBE.cuh:1-8).  Uploads g first when it
+ * is not resident. */
+MBE_API mbe_status mbe_enumerate(mbe_ctx* ctx, const mbe_graph* g, mbe_variant variant,
+                         const mbe_opts* opts, mbe_result* out);
+
+/* Batched enumeration: n graphs in one persistent launch.  Per-graph
+ * results go to out[i].  No reference counterpart: the reference runs one
+ * graph per process (src/main.cu:9). */
+MBE_API mbe_status mbe_batch_run(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n,
+                         mbe_variant variant, const mbe_opts* opts,
+                         mbe_result* out, float* total_ms);
+
+/* Canonical per-biclique hash: rows A and cols B in file orientation, in
+ * any order.  The graph hash is the wrapping sum of this over bicliques. */
+MBE_API uint64_t mbe_biclique_hash(const uint32_t* rows, uint32_t n_rows,
+                           const uint32_t* cols, uint32_t n_cols);
+
+MBE_API const char* mbe_variant_name(mbe_variant v);
+/* Maps a CLI algorithm string to a variant; unknown strings map to
+ * MBE_CUMBE as src/main.cu:122 does. */
+MBE_API mbe_variant mbe_variant_from_name(const char* name);
+
+/* Launch geometry of the last enumeration on ctx (the CLI's grid_size line). */
+MBE_API mbe_status mbe_ctx_last_grid(mbe_ctx* ctx, uint32_t* grid_expand, uint32_t* grid_dfs, uint32_t* block);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MBE_H_ */

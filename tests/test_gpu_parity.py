@@ -1,0 +1,117 @@
+"""GPU parity: libmbe's sm_103a kernels against the CPU oracle (count and
+canonical hash bit-exact), through the C ABI."""
+import os
+
+import numpy as np
+import pytest
+
+import cumbe_gb300 as cm
+import oracle
+from conftest import random_csr
+
+pytestmark = pytest.mark.gpu
+VARIANTS = ["cuMBE", "noRS", "noES", "noWS"]
+
+
+def _check(engine, g, variant="cuMBE", **kw):
+    nr, nc, rp, ci = g
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=4, **kw)
+    G = cm.Graph.from_csr(nr, nc, rp, ci)
+    got = engine.enumerate(G, variant, **kw)
+    assert (got.count, got.hash) == (want.count, want.hash), (variant, kw, got, want)
+    return got
+
+
+def test_tiny_random_all_variants(engine):
+    rng = np.random.default_rng(11)
+    for _ in range(60):
+        g = random_csr(rng, int(rng.integers(1, 14)), int(rng.integers(1, 14)), rng.uniform(0.05, 0.95))
+        for v in VARIANTS:
+            _check(engine, g, v)
+
+
+@pytest.mark.parametrize("shape", [(60, 40, 0.12), (40, 60, 0.2), (120, 90, 0.05), (33, 70, 0.5)])
+def test_medium_random(engine, shape):
+    rng = np.random.default_rng(hash(shape) & 0xFFFF)
+    g = random_csr(rng, *shape)
+    for v in VARIANTS:
+        _check(engine, g, v)
+
+
+def test_edge_cases(engine):
+    cases = [
+        (3, 4, np.zeros(4, np.uint64), np.zeros(0, np.uint32)),
+        (1, 1, np.array([0, 1], np.uint64), np.array([0], np.uint32)),
+        (3, 5, np.array([0, 5, 10, 15], np.uint64), np.tile(np.arange(5, dtype=np.uint32), 3)),
+        (4, 3, np.array([0, 1, 1, 2, 2], np.uint64), np.array([0, 2], np.uint32)),
+        (0, 3, np.zeros(1, np.uint64), np.zeros(0, np.uint32)),
+        (40, 1, np.arange(41, dtype=np.uint64), np.zeros(40, np.uint32)),
+    ]
+    for g in cases:
+        for v in VARIANTS:
+            _check(engine, g, v)
+
+
+def test_config0_synthetic(engine):
+    """|U|=2000, |V|=1000, 10,000 Chung-Lu edges (gamma 2.1), seed 1."""
+    G = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    nr, nc, rp, ci = G.csr()
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=8)
+    for v in VARIANTS:
+        got = engine.enumerate(G, v)
+        assert (got.count, got.hash) == (want.count, want.hash), v
+
+
+def test_thresholds(engine):
+    rng = np.random.default_rng(5)
+    g = random_csr(rng, 80, 50, 0.15)
+    for a, b in [(1, 1), (2, 2), (3, 1), (1, 4), (4, 4)]:
+        _check(engine, g, "cuMBE", min_rows=a, min_cols=b)
+
+
+def test_batch_matches_single(engine):
+    rng = np.random.default_rng(9)
+    gs, want = [], []
+    for i in range(40):
+        g = random_csr(rng, int(rng.integers(2, 70)), int(rng.integers(2, 70)), rng.uniform(0.02, 0.3))
+        gs.append(cm.Graph.from_csr(*g))
+        want.append(oracle.ref_enumerate(*g))
+    res, ms = engine.batch(gs)
+    for r, w in zip(res, want):
+        assert (r.count, r.hash) == (w.count, w.hash)
+
+
+def test_small_pool_forces_chunks(engine):
+    """A tiny node pool makes the root expansion run in many chunks with
+    retries; results must not change."""
+    G = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    nr, nc, rp, ci = G.csr()
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=8)
+    old = os.environ.get("MBE_POOL_MB")
+    os.environ["MBE_POOL_MB"] = "2"
+    try:
+        got = engine.enumerate(G)
+    finally:
+        if old is None:
+            del os.environ["MBE_POOL_MB"]
+        else:
+            os.environ["MBE_POOL_MB"] = old
+    assert (got.count, got.hash) == (want.count, want.hash)
+
+
+def test_small_arena_spills_to_pool(engine):
+    """A 4096-word DFS arena forces child records into the shared node pool
+    and donations to replay deep paths; results must not change."""
+    G = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    nr, nc, rp, ci = G.csr()
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=8)
+    got = engine.enumerate(G, stack_words=4096)
+    assert (got.count, got.hash) == (want.count, want.hash)
+
+
+def test_donation_granularity_does_not_change_results(engine):
+    G = cm.Graph.generate(3000, 1500, 16000, 2.0, 2.2, 0, 4)
+    base = engine.enumerate(G, "noWS")
+    for dm in (2, 3, 8, 64):
+        got = engine.enumerate(G, "cuMBE", donate_min=dm)
+        assert (got.count, got.hash) == (base.count, base.hash), dm
