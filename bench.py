@@ -1,0 +1,292 @@
+"""Throughput benchmark: maximal biclique enumeration on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload power_law_94k_30k]
+
+A step is one full enumeration (count + canonical hash) of the workload
+graph.  Prints ONE JSON line (rank 0).
+
+  value      maximal bicliques/sec with the graph resident in HBM: the sum
+             of counts over the K timed steps / the sum of the steps' device
+             time (CUDA events on the library's stream around the root
+             expansion and DFS kernels); L2 is flushed (a 512 MiB write)
+             before every timed step.
+  e2e        the same metric through the public C ABI from host buffers:
+             every step drops the device copy, then mbe_enumerate uploads
+             (host->device copies, transpose, root order), enumerates and
+             copies the result back; wall-clock per step.
+  roofline   dfs_kernel's algorithmic bytes (4 B x 32-bit words of bit rows
+             and candidate data it streams, counted by the kernel) / its
+             event time, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a restatement of the reference's search) on
+             the host cores over a stride sample of the same graph's roots.
+
+`--impl reference` times that CPU restatement alone (the reference ships
+no CPU implementation of this path; its GPU kernels cannot be installed
+as a package), on the same metric, one stride sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# The workloads (synthetic, seeded).  The default is the one the headline
+# metric is quoted on: a 94,000 x 30,000 power-law bipartite graph.
+WORKLOADS = {
+    "power_law_94k_30k": dict(n_rows=94000, n_cols=30000, n_edges=293000, gamma_rows=2.0, gamma_cols=2.3,
+                              max_deg=7500, seed=2, cpu_stride=1000),
+    # same generator with 100k edges: the small case ncu captures run on
+    "power_law_94k_30k_e100k": dict(n_rows=94000, n_cols=30000, n_edges=100000, gamma_rows=2.0, gamma_cols=2.3,
+                                    max_deg=7500, seed=2, cpu_stride=100),
+    "power_law_2k_1k": dict(n_rows=2000, n_cols=1000, n_edges=10000, gamma_rows=2.1, gamma_cols=2.1,
+                            max_deg=0, seed=1, cpu_stride=1),
+}
+DEFAULT_WORKLOAD = "power_law_94k_30k"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(workload):
+    """Per-launch DRAM bytes of dfs_kernel from the committed ncu summary
+    (profiles/dfs_kernel_<workload>.md, line 'traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", f"dfs_kernel_{workload}.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if not self.rows:
+            return None
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(g, wl, threads, stride_mult=1):
+    """The oracle port on the host cores over a stride sample of the roots."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    nr, nc, rp, ci = g.csr()
+    stride = wl["cpu_stride"] * stride_mult
+    t0 = time.perf_counter()
+    r = oracle.ref_enumerate_sampled(nr, nc, rp, ci, stride, threads=threads)
+    dt = time.perf_counter() - t0
+    return r, dt, stride
+
+
+def run_reference(args, wl, rank, world):
+    """--impl reference: the CPU restatement of the reference's search."""
+    if rank != 0:
+        return
+    import cumbe_gb300 as cm
+    from cumbe_gb300 import build as b
+    b.build()
+    params = {k: v for k, v in wl.items() if k != "cpu_stride"}
+    g = cm.Graph.generate(**params)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(g, wl, threads, stride_mult=10)  # warm caches on a 10x thinner sample
+    tot_c, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        r, dt, stride = cpu_baseline(g, wl, threads)
+        tot_c += r.count
+        tot_t += dt
+    v = tot_c / tot_t if tot_t > 0 else 0.0
+    sample = (f"every {stride}-th root in processing order (stride sample) of the {args.workload} graph, "
+              f"{threads} threads")
+    line = {"impl": "reference", "metric": "maximal bicliques/sec", "value": v, "unit": "bicliques/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot_t * 1000 / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": args.workload, **params, "variant": "cuMBE"},
+            "cpu_baseline": {"value": v, "unit": "bicliques/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "bicliques/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--variant", default="cuMBE", choices=["cuMBE", "noRS", "noES", "noWS"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist_env()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+        return
+
+    import torch
+    import cumbe_gb300 as cm
+    from cumbe_gb300 import build as b
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    b.build()
+    torch.cuda.set_device(local)
+    params = {k: v for k, v in wl.items() if k != "cpu_stride"}
+    g = cm.Graph.generate(**params)
+    info = g.info()
+    eng = cm.Engine(local)
+    eng.upload(g)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        r0 = eng.enumerate(g, args.variant)
+    # ---- device-resident throughput (value) ----
+    c0 = eng.counters()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    tot_count, tot_ms, tot_dfs_ms, tot_words = 0, 0.0, 0.0, 0
+    results = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r = eng.enumerate(g, args.variant)
+        results.append(r)
+        tot_count += r.count
+        tot_ms += r.ms
+        tot_dfs_ms += r.ms - r.ms_prep
+        tot_words += r.words
+    barrier()
+    clocks = sampler.stop()
+    c1 = eng.counters()
+    if any((x.count, x.hash) != (r0.count, r0.hash) for x in results):
+        raise SystemExit("enumeration results differ between steps")
+    ms_step = tot_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = tot_count * world / (ms_step * args.steps / 1000.0)
+
+    # ---- end to end through the C ABI from host buffers (e2e) ----
+    e_c0 = eng.counters()
+    barrier()
+    e2e_wall, e2e_count = 0.0, 0
+    for _ in range(args.steps):
+        eng.release(g)
+        t0 = time.perf_counter()
+        r = eng.enumerate(g, args.variant)  # upload (H2D + transpose) + enumerate + D2H
+        e2e_wall += time.perf_counter() - t0
+        e2e_count += r.count
+    barrier()
+    e_c1 = eng.counters()
+    e2e = {"value": e2e_count * world / e2e_wall, "unit": "bicliques/s",
+           "h2d_bytes_per_step": (e_c1["h2d"] - e_c0["h2d"]) // args.steps,
+           "d2h_bytes_per_step": (e_c1["d2h"] - e_c0["d2h"]) // args.steps}
+
+    # ---- roofline of the dominant kernel (dfs_kernel) ----
+    peak, peak_kind = peak_hbm()
+    achieved = (tot_words * 4) / (tot_dfs_ms / 1000.0) / 1e9 if tot_dfs_ms > 0 else 0.0
+    traffic = profile_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind, "kernel": "dfs_kernel",
+                "algorithmic_bytes_per_launch": tot_words * 4 // args.steps,
+                "launch_ms": tot_dfs_ms / args.steps}
+
+    line = {"metric": "maximal bicliques/sec", "value": value, "unit": "bicliques/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": args.workload, **params, "variant": args.variant,
+                       "l2": "flushed before every timed step (512 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "bicliques_per_step": r0.count, "hash": f"{r0.hash:#018x}",
+                       "tree_nodes_per_step": r0.nodes, "n_edges": info["n_edges"]},
+            "e2e": e2e, "roofline": roofline,
+            "gpu_launches": c1["launches"] - c0["launches"],
+            "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rc, dt, stride = cpu_baseline(g, wl, threads)
+        line["cpu_baseline"] = {"value": rc.count / dt if dt > 0 else 0.0, "unit": "bicliques/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"every {stride}-th root (stride sample) of the same graph: "
+                                          f"{rc.count} bicliques in {dt:.2f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

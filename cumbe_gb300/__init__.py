@@ -62,8 +62,8 @@ class _Opts(ctypes.Structure):
 
 class _Result(ctypes.Structure):
     _fields_ = [("count", ctypes.c_uint64), ("hash", ctypes.c_uint64), ("nodes", ctypes.c_uint64),
-                ("words", ctypes.c_uint64), ("emitted", ctypes.c_uint64), ("ms", ctypes.c_float),
-                ("ms_prep", ctypes.c_float)]
+                ("words", ctypes.c_uint64), ("words_expand", ctypes.c_uint64), ("emitted", ctypes.c_uint64),
+                ("ms", ctypes.c_float), ("ms_prep", ctypes.c_float)]
 
 
 # Every symbol include/mbe.h declares, with its ctypes signature.
@@ -90,6 +90,7 @@ SIGNATURES = {
     "mbe_variant_name": (ctypes.c_char_p, [ctypes.c_int]),
     "mbe_variant_from_name": (ctypes.c_int, [ctypes.c_char_p]),
     "mbe_ctx_last_grid": (ctypes.c_int, [_VP, _U32P, _U32P, _U32P]),
+    "mbe_ctx_counters": (ctypes.c_int, [_VP, _U64P, _U64P, _U64P]),
 }
 
 _lib = None
@@ -121,6 +122,7 @@ class Result:
     hash: int
     nodes: int
     words: int
+    words_expand: int
     ms: float
     ms_prep: float
     bicliques: list | None = field(default=None, repr=False)
@@ -239,7 +241,7 @@ class Engine:
         r = _Result()
         _check(lib().mbe_enumerate(self._h, g.handle, VARIANTS[variant], ctypes.byref(o), ctypes.byref(r)),
                "mbe_enumerate")
-        return Result(r.count, r.hash, r.nodes, r.words, r.ms, r.ms_prep)
+        return Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep)
 
     def batch(self, graphs: list[Graph], variant: str = "cuMBE", min_rows: int = 0, min_cols: int = 0,
               **tuning) -> tuple[list[Result], float]:
@@ -250,7 +252,14 @@ class Engine:
         o = _opts(flags=OPT_TIMING, min_rows=min_rows, min_cols=min_cols, **tuning)
         _check(lib().mbe_batch_run(self._h, arr, n, VARIANTS[variant], ctypes.byref(o), res, ctypes.byref(tot)),
                "mbe_batch_run")
-        return [Result(r.count, r.hash, r.nodes, r.words, r.ms, r.ms_prep) for r in res], tot.value
+        return [Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep) for r in res], tot.value
+
+    def counters(self) -> dict:
+        """Cumulative kernel launches and host<->device bytes of this context."""
+        l, h, d = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().mbe_ctx_counters(self._h, ctypes.byref(l), ctypes.byref(h), ctypes.byref(d)),
+               "mbe_ctx_counters")
+        return {"launches": l.value, "h2d": h.value, "d2h": d.value}
 
     def last_grid(self):
         a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()

@@ -20,6 +20,7 @@ struct mbe_ctx {
     std::unordered_map<uint64_t, DeviceGraph> resident;
     EngineBuffers eb;
     EngineStats last_stats;
+    IoCounters io;
     std::mutex mu;
 };
 
@@ -41,7 +42,7 @@ mbe_status ensure_resident(mbe_ctx* ctx, const mbe_graph* g, const DeviceGraph**
         return MBE_OK;
     }
     DeviceGraph d;
-    mbe_status st = build_device_graph(g, ctx->stream, ctx->n_sm, &d);
+    mbe_status st = build_device_graph(g, ctx->stream, ctx->n_sm, &d, &ctx->io);
     if (st != MBE_OK) return st;
     auto res = ctx->resident.emplace(g->uid, std::move(d));
     *out = &res.first->second;
@@ -149,7 +150,7 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         });
     // Thresholds are stated in file orientation; a batch mixing orientations
     // is enumerated per orientation group.
-    std::vector<ResultAcc> acc(n, ResultAcc{0, 0, 0, 0});
+    std::vector<ResultAcc> acc(n, ResultAcc{});
     float ms = 0;
     EngineStats stats;
     bool thresholds = opts && (opts->min_rows || opts->min_cols);
@@ -165,13 +166,14 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         EngineConfig cfg = make_config(variant, opts, sw);
         std::vector<ResultAcc> part;
         EngineStats ps;
-        st = engine_run(ctx->eb, ctx->stream, cfg, devs, use, part, &ps);
+        st = engine_run(ctx->eb, ctx->stream, cfg, devs, use, part, &ps, &ctx->io);
         if (st != MBE_OK) return st;
         for (uint32_t i = 0; i < n; i++) {
             acc[i].count += part[i].count;
             acc[i].hash += part[i].hash;
             acc[i].nodes += part[i].nodes;
             acc[i].words += part[i].words;
+            acc[i].words_expand += part[i].words_expand;
         }
         ms += ps.ms_expand + ps.ms_dfs;
         stats.ms_expand += ps.ms_expand;
@@ -189,6 +191,7 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         r.hash = (opts && (opts->flags & MBE_OPT_NO_HASH)) ? 0 : acc[i].hash;
         r.nodes = acc[i].nodes;
         r.words = acc[i].words;
+        r.words_expand = acc[i].words_expand;
         r.ms = stats.ms_expand + stats.ms_dfs;
         r.ms_prep = stats.ms_expand;
     }
@@ -210,6 +213,16 @@ extern "C" mbe_status mbe_batch_run(mbe_ctx* ctx, const mbe_graph* const* graphs
     if (!ctx || (!graphs && n) || (!out && n)) return fail(MBE_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(ctx->mu);
     return run_graphs(ctx, graphs, n, variant, opts, out, total_ms);
+}
+
+extern "C" mbe_status mbe_ctx_counters(mbe_ctx* ctx, uint64_t* launches, uint64_t* h2d, uint64_t* d2h) {
+    clear_error();
+    if (!ctx) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (launches) *launches = ctx->io.launches;
+    if (h2d) *h2d = ctx->io.h2d;
+    if (d2h) *d2h = ctx->io.d2h;
+    return MBE_OK;
 }
 
 // Launch geometry of the last enumeration (CLI "grid_size" line).

@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                 ResultAcc* r = &a.results[rt.x];
                 unsigned long long words = s_scan * (rs ? 3 : 2) + d;
                 atomicAdd(&r->nodes, 1ull);
-                atomicAdd(&r->words, words);
+                atomicAdd(&r->words_expand, words);
                 if (!s_nonmax && nRset >= a.minR) {
                     unsigned long long sR = G.eR[x] + s_sabs;
                     atomicAdd(&r->count, 1ull);
@@ -630,7 +630,7 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
                                ResultAcc& acc_out, bool replay) {
     // a replayed evaluation re-derives a donated node: its counts belong to
     // the donor and are discarded
-    ResultAcc scratch_acc{0, 0, 0, 0};
+    ResultAcc scratch_acc{};
     ResultAcc& acc = replay ? scratch_acc : acc_out;
     const unsigned lane = lane_id();
     const NodeHdr* h = (const NodeHdr*)nd;
@@ -902,7 +902,7 @@ __device__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
         if (acc.nodes) atomicAdd(&r->nodes, acc.nodes);
         if (acc.words) atomicAdd(&r->words, acc.words);
     }
-    acc = ResultAcc{0, 0, 0, 0};
+    acc = ResultAcc{};
 }
 
 __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
@@ -925,7 +925,7 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
     const bool donate = a.variant != MBE_NOWS;
-    ResultAcc acc{0, 0, 0, 0};
+    ResultAcc acc{};
     uint32_t evals = 0;
     Task t{};
     uint32_t my_path = 0;
@@ -1078,9 +1078,9 @@ struct Ctrl {
 
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
                       const std::vector<const DeviceGraph*>& gs, const std::vector<uint2>& roots,
-                      std::vector<ResultAcc>& results, EngineStats* stats) {
+                      std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io) {
     const uint32_t ng = (uint32_t)gs.size();
-    results.assign(ng, ResultAcc{0, 0, 0, 0});
+    results.assign(ng, ResultAcc{});
     if (ng == 0 || roots.empty()) return MBE_OK;
     uint32_t maxNR = 1, maxW = 1;
     for (const DeviceGraph* g : gs) {
@@ -1107,19 +1107,19 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     const uint32_t q_margin = nwarpsB + 1024;
     const uint32_t task_cap = (uint32_t)std::min<size_t>(roots.size() + q_margin + (size_t)cfg.extra_tasks, 0x7FFFFFFF);
     const uint32_t max_frames = cfg.max_frames;
-    // Arena and node pool are sized once per context from free device
-    // memory: per-warp DFS arenas take ~30% of it (at most 16 MiB each), the
-    // shared node pool ~15% (at most 32 GiB).
-    if (!eb.arena_words || !eb.pool_words) {
-        size_t fr = 0, tot = 0;
-        MBE_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
-        uint64_t per_warp = (uint64_t)(fr * 0.30) / nwarpsB / 4;
-        eb.arena_words = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(per_warp, 1u << 16), 1u << 22) & ~31u;
-        uint64_t pool = (uint64_t)(fr * 0.15) / 4;
-        eb.pool_words = std::min<uint64_t>(std::max<uint64_t>(pool, 1ull << 26), 1ull << 33) & ~31ull;
+    // Per-warp DFS arenas default to 4 MiB each (at most 30% of free device
+    // memory in total); the shared node pool starts at 2 GiB and is doubled
+    // (up to 60% of free memory) whenever a run exhausts it.
+    size_t free_b = 0, tot_b = 0;
+    MBE_CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
+    if (!eb.arena_words) {
+        uint64_t cap = (uint64_t)(free_b * 0.30) / nwarpsB / 4;
+        uint64_t want = 1u << 20;
+        if (const char* env = std::getenv("MBE_ARENA_WORDS")) want = std::strtoull(env, nullptr, 10);
+        eb.arena_words = (uint32_t)std::max<uint64_t>(std::min(want, cap), 1u << 14) & ~31u;
     }
+    if (!eb.pool_words) eb.pool_words = 1ull << 29;
     const uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
-    const uint64_t pool_words = cfg.pool_words ? std::min<uint64_t>(cfg.pool_words, eb.pool_words) : eb.pool_words;
     const uint32_t retry_cap = 1u << 16;
 
     mbe_status st;
@@ -1135,16 +1135,13 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     if ((st = eb.a_cl.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
     if ((st = eb.a_cnt.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
     if ((st = eb.a_keys.ensure(sizeof(unsigned long long) * (size_t)gridA * keys_cap))) return st;
-    if ((st = eb.pool.ensure(sizeof(uint32_t) * eb.pool_words))) return st;
     if ((st = eb.arena.ensure(sizeof(uint32_t) * (size_t)nwarpsB * eb.arena_words))) return st;
     if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * max_frames))) return st;
     if ((st = eb.results.ensure(sizeof(ResultAcc) * ng))) return st;
     if ((st = eb.retry_in.ensure(sizeof(uint32_t) * (size_t)retry_cap))) return st;
-    // cmap must be all -1 at kernel entry; kernels restore it after each root
-    MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));
     MBE_CUDA_TRY(cudaMemcpyAsync(eb.graphs.ptr, views.data(), sizeof(GraphView) * ng, cudaMemcpyHostToDevice, s));
     MBE_CUDA_TRY(cudaMemcpyAsync(eb.roots.ptr, roots.data(), sizeof(uint2) * roots.size(), cudaMemcpyHostToDevice, s));
-    MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
+    io->h2d += sizeof(GraphView) * ng + sizeof(uint2) * roots.size();
 
     Ctrl* ctrl = (Ctrl*)eb.ctrl.ptr;
     EngineArgs a;
@@ -1155,16 +1152,11 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.minL = cfg.minL;
     a.minR = cfg.minR;
     a.donate_min = std::max(2u, cfg.donate_min);
-    a.roots = (const uint2*)eb.roots.ptr;
-    a.n_roots = (uint32_t)roots.size();
     a.root_next = &ctrl->root_next;
     a.retry = (uint32_t*)eb.retry_in.ptr;
     a.n_retry = &ctrl->n_retry;
     a.retry_cap = retry_cap;
-    a.pool = (uint32_t*)eb.pool.ptr;
-    a.pool_words = pool_words;
     a.pool_top = &ctrl->pool_top;
-    a.pool_watermark = pool_words / 2;
     a.tasks = (Task*)eb.tasks.ptr;
     a.ready = (uint32_t*)eb.ready.ptr;
     a.task_cap = task_cap;
@@ -1180,21 +1172,17 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.a_keys = (unsigned long long*)eb.a_keys.ptr;
     a.maxNR = maxNR;
     a.keys_cap = keys_cap;
+    a.max_n = &ctrl->max_n;
     a.arena = (uint32_t*)eb.arena.ptr;
     a.arena_words = arena_words;
     a.frames = (Frame*)eb.frames.ptr;
     a.max_frames = max_frames;
-    a.max_n = &ctrl->max_n;
     a.max_W = maxW;
     a.results = (ResultAcc*)eb.results.ptr;
     a.error = &ctrl->error;
     a.error_info = &ctrl->error_info;
     a.timeout_ns = cfg.timeout_ns;
 
-    // Roots that did not fit the pool in one chunk are retried first in the
-    // next chunk (from a host copy), then the main list resumes.
-    std::vector<uint2> pending_roots;  // retry roots carried to the next chunk
-    uint32_t main_next = 0;
     cudaEvent_t e0, e1, e2;
     MBE_CUDA_TRY(cudaEventCreate(&e0));
     MBE_CUDA_TRY(cudaEventCreate(&e1));
@@ -1202,92 +1190,137 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     float ms_a = 0, ms_b = 0;
     uint32_t chunks = 0;
     mbe_status result = MBE_OK;
-    while (result == MBE_OK && (main_next < roots.size() || !pending_roots.empty())) {
-        chunks++;
-        // Chunk root list: retried roots, then the main list from main_next.
-        const uint2* list;
-        uint32_t list_n;
-        std::vector<uint2> chunk_list;
-        if (!pending_roots.empty()) {
-            chunk_list = pending_roots;
-            list_n = (uint32_t)chunk_list.size();
-            if ((st = eb.retry_list.ensure(sizeof(uint2) * list_n))) return st;
-            MBE_CUDA_TRY(cudaMemcpyAsync(eb.retry_list.ptr, chunk_list.data(), sizeof(uint2) * list_n,
-                                         cudaMemcpyHostToDevice, s));
-            list = (const uint2*)eb.retry_list.ptr;
-        } else {
-            list = (const uint2*)eb.roots.ptr + main_next;
-            list_n = (uint32_t)roots.size() - main_next;
-        }
-        a.roots = list;
-        a.n_roots = list_n;
-        MBE_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
-        MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
-        MBE_CUDA_TRY(cudaEventRecord(e0, s));
-        expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
-        MBE_CUDA_TRY(cudaGetLastError());
-        MBE_CUDA_TRY(cudaEventRecord(e1, s));
-        // DFS scratch is laid out for the largest record this chunk made
-        uint32_t max_n = 0;
-        MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
-        MBE_CUDA_TRY(cudaStreamSynchronize(s));
-        {
-            uint32_t scr_n = std::max<uint32_t>(max_n, 32);
-            size_t kc = 32;
-            while (kc < scr_n) kc <<= 1;
-            size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc, 32);
-            if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
-            a.scratch = (uint32_t*)eb.scratch.ptr;
-            a.scratch_words = (uint32_t)sw;
-            a.scr_n = scr_n;
-            a.scr_kc = (uint32_t)kc;
-        }
-        dfs_kernel<<<gridB, kThreadsB, 0, s>>>(a);
-        MBE_CUDA_TRY(cudaGetLastError());
-        MBE_CUDA_TRY(cudaEventRecord(e2, s));
-        Ctrl hc;
-        MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
-        MBE_CUDA_TRY(cudaStreamSynchronize(s));
-        float t1 = 0, t2 = 0;
-        cudaEventElapsedTime(&t1, e0, e1);
-        cudaEventElapsedTime(&t2, e1, e2);
-        ms_a += t1;
-        ms_b += t2;
-        if (hc.error) {
-            static const char* names[] = {"none", "node pool exhausted", "task queue full", "device wait timed out",
-                                          "search deeper than the frame stack", "scratch too small"};
-            mbe_status code = hc.error == kErrTimeout ? MBE_ERR_DEVICE_TIMEOUT
-                              : hc.error == kErrPool  ? MBE_ERR_OUT_OF_MEMORY
-                                                      : MBE_ERR_CAPACITY;
-            result = fail(code, std::string("enumeration kernel: ") + names[hc.error < 6 ? hc.error : 0] +
-                                    " (info " + std::to_string(hc.error_info) + ")");
+    for (int attempt = 0;; attempt++) {
+        // The node pool grows by doubling when a run exhausts it (up to 60% of
+        // free device memory); a fixed cap (cfg.pool_words) disables growth.
+        const uint64_t pool_words = cfg.pool_words ? std::min<uint64_t>(cfg.pool_words, eb.pool_words) : eb.pool_words;
+        if ((st = eb.pool.ensure(sizeof(uint32_t) * eb.pool_words))) {
+            result = st;
             break;
         }
-        uint32_t consumed = std::min(hc.root_next, list_n);
-        std::vector<uint32_t> retry_idx(std::min(hc.n_retry, retry_cap));
-        if (!retry_idx.empty())
-            MBE_CUDA_TRY(cudaMemcpy(retry_idx.data(), a.retry, sizeof(uint32_t) * retry_idx.size(),
-                                    cudaMemcpyDeviceToHost));
-        if (hc.n_retry > retry_cap || consumed == 0 || consumed == (uint32_t)retry_idx.size()) {
-            // nothing fitted an empty pool: more chunks would not help
-            result = fail(MBE_ERR_OUT_OF_MEMORY, "a root's search record does not fit the node pool");
-            break;
+        a.pool = (uint32_t*)eb.pool.ptr;
+        a.pool_words = pool_words;
+        a.pool_watermark = pool_words / 2;
+        MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));  // kernels restore -1 after each root
+        MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
+        ms_a = ms_b = 0;
+        chunks = 0;
+        result = MBE_OK;
+        bool pool_exhausted = false;
+        // Roots that did not fit the pool in one chunk are retried first in
+        // the next chunk (from a host copy), then the main list resumes.
+        std::vector<uint2> pending_roots;
+        uint32_t main_next = 0;
+        while (main_next < roots.size() || !pending_roots.empty()) {
+            chunks++;
+            const uint2* list;
+            uint32_t list_n;
+            std::vector<uint2> chunk_list;
+            if (!pending_roots.empty()) {
+                chunk_list = pending_roots;
+                list_n = (uint32_t)chunk_list.size();
+                if ((st = eb.retry_list.ensure(sizeof(uint2) * list_n))) return st;
+                MBE_CUDA_TRY(cudaMemcpyAsync(eb.retry_list.ptr, chunk_list.data(), sizeof(uint2) * list_n,
+                                             cudaMemcpyHostToDevice, s));
+                io->h2d += sizeof(uint2) * list_n;
+                list = (const uint2*)eb.retry_list.ptr;
+            } else {
+                list = (const uint2*)eb.roots.ptr + main_next;
+                list_n = (uint32_t)roots.size() - main_next;
+            }
+            a.roots = list;
+            a.n_roots = list_n;
+            MBE_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
+            MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
+            MBE_CUDA_TRY(cudaEventRecord(e0, s));
+            expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
+            MBE_CUDA_TRY(cudaGetLastError());
+            MBE_CUDA_TRY(cudaEventRecord(e1, s));
+            // DFS scratch is laid out for the largest record this chunk made
+            uint32_t max_n = 0;
+            MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
+            MBE_CUDA_TRY(cudaStreamSynchronize(s));
+            io->d2h += sizeof max_n;
+            {
+                uint32_t scr_n = std::max<uint32_t>(max_n, 32);
+                size_t kc = 32;
+                while (kc < scr_n) kc <<= 1;
+                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc, 32);
+                if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
+                a.scratch = (uint32_t*)eb.scratch.ptr;
+                a.scratch_words = (uint32_t)sw;
+                a.scr_n = scr_n;
+                a.scr_kc = (uint32_t)kc;
+            }
+            dfs_kernel<<<gridB, kThreadsB, 0, s>>>(a);
+            MBE_CUDA_TRY(cudaGetLastError());
+            MBE_CUDA_TRY(cudaEventRecord(e2, s));
+            io->launches += 2;
+            Ctrl hc;
+            MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            MBE_CUDA_TRY(cudaStreamSynchronize(s));
+            io->d2h += sizeof(Ctrl);
+            float t1 = 0, t2 = 0;
+            cudaEventElapsedTime(&t1, e0, e1);
+            cudaEventElapsedTime(&t2, e1, e2);
+            ms_a += t1;
+            ms_b += t2;
+            if (hc.error) {
+                static const char* names[] = {"none",
+                                              "node pool exhausted",
+                                              "task queue full",
+                                              "device wait timed out",
+                                              "search deeper than the frame stack",
+                                              "scratch too small",
+                                              "donated path did not re-derive"};
+                if (hc.error == kErrPool) pool_exhausted = true;
+                mbe_status code = hc.error == kErrTimeout ? MBE_ERR_DEVICE_TIMEOUT
+                                  : hc.error == kErrPool  ? MBE_ERR_OUT_OF_MEMORY
+                                                          : MBE_ERR_CAPACITY;
+                result = fail(code, std::string("enumeration kernel: ") + names[hc.error < 7 ? hc.error : 0] +
+                                        " (info " + std::to_string(hc.error_info) + ")");
+                break;
+            }
+            uint32_t consumed = std::min(hc.root_next, list_n);
+            std::vector<uint32_t> retry_idx(std::min(hc.n_retry, retry_cap));
+            if (!retry_idx.empty()) {
+                MBE_CUDA_TRY(cudaMemcpy(retry_idx.data(), a.retry, sizeof(uint32_t) * retry_idx.size(),
+                                        cudaMemcpyDeviceToHost));
+                io->d2h += sizeof(uint32_t) * retry_idx.size();
+            }
+            if (hc.n_retry > retry_cap || consumed == 0 || consumed == (uint32_t)retry_idx.size()) {
+                // nothing fitted an empty pool: more chunks would not help
+                pool_exhausted = true;
+                result = fail(MBE_ERR_OUT_OF_MEMORY, "a root's search record does not fit the node pool");
+                break;
+            }
+            std::vector<uint2> next_pending;
+            const uint2* host_list = pending_roots.empty() ? roots.data() + main_next : chunk_list.data();
+            for (uint32_t r : retry_idx) next_pending.push_back(host_list[r]);
+            if (!pending_roots.empty()) {
+                for (uint32_t r = consumed; r < list_n; r++) next_pending.push_back(chunk_list[r]);
+            } else {
+                main_next += consumed;
+            }
+            pending_roots.swap(next_pending);
         }
-        std::vector<uint2> next_pending;
-        const uint2* host_list = pending_roots.empty() ? roots.data() + main_next : chunk_list.data();
-        for (uint32_t r : retry_idx) next_pending.push_back(host_list[r]);
-        if (!pending_roots.empty()) {
-            for (uint32_t r = consumed; r < list_n; r++) next_pending.push_back(chunk_list[r]);
-        } else {
-            main_next += consumed;
+        if (pool_exhausted && !cfg.pool_words) {
+            size_t fr = 0, tt = 0;
+            MBE_CUDA_TRY(cudaMemGetInfo(&fr, &tt));
+            uint64_t limit_words = (uint64_t)((fr + eb.pool.bytes) * 0.60) / 4;
+            if (eb.pool_words * 2 <= limit_words) {
+                eb.pool_words *= 2;
+                continue;
+            }
         }
-        pending_roots.swap(next_pending);
+        break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
     if (result != MBE_OK) return result;
     MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
+    io->d2h += sizeof(ResultAcc) * ng;
     if (stats) {
         stats->ms_expand = ms_a;
         stats->ms_dfs = ms_b;

@@ -77,7 +77,7 @@ struct Frame {
 };
 
 struct ResultAcc {
-    unsigned long long count, hash, nodes, words;
+    unsigned long long count, hash, nodes, words, words_expand;
 };
 
 enum : int {

@@ -33,8 +33,8 @@ struct EngineConfig {
     uint32_t donate_min = 2;
     uint32_t blocks_per_sm = 0;         // 0 = occupancy limit
     uint32_t max_frames = 512;
-    uint32_t arena_words = 0;           // per warp; 0 = sized from free memory
-    uint64_t pool_words = 0;            // node pool; 0 = sized from free memory
+    uint32_t arena_words = 0;           // per warp; 0 = engine default
+    uint64_t pool_words = 0;            // node pool cap; 0 = engine default (grows on demand)
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
     unsigned long long timeout_ns = 60ull * 1000000000ull;
 };
@@ -48,6 +48,6 @@ struct EngineStats {
 // receives the accumulated count / hash / nodes / words of graph g.
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
                       const std::vector<const DeviceGraph*>& graphs, const std::vector<uint2>& roots,
-                      std::vector<ResultAcc>& results, EngineStats* stats);
+                      std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io);
 
 }  // namespace mbe

@@ -256,18 +256,29 @@ __global__ void elem_hashes(uint32_t nR, uint32_t nL, const uint32_t* r_orig, in
 
 cudaError_t build_csr(uint32_t n_keys, uint64_t n_edges, const uint32_t* keys, const uint32_t* vals, uint32_t* ptr,
                       uint32_t* adj, uint32_t* cursor, uint32_t* scan_tmp, uint32_t max_val, uint32_t* bitmaps,
-                      uint32_t n_bitmaps, int n_sm, cudaStream_t s) {
+                      uint32_t n_bitmaps, int n_sm, cudaStream_t s, IoCounters* io) {
     cudaError_t err;
     if ((err = cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * ((size_t)n_keys + 1), s))) return err;
     int grid = n_sm * 8;
-    if (n_edges) count_keys<<<grid, 256, 0, s>>>(keys, n_edges, cursor);
+    if (n_edges) {
+        count_keys<<<grid, 256, 0, s>>>(keys, n_edges, cursor);
+        io->launches++;
+    }
     if ((err = exclusive_scan_u32(cursor, ptr, n_keys + 1, scan_tmp, nullptr, s))) return err;
+    io->launches += 3;
     if ((err = cudaMemcpyAsync(cursor, ptr, sizeof(uint32_t) * n_keys, cudaMemcpyDeviceToDevice, s))) return err;
-    if (n_edges) scatter_keys<<<grid, 256, 0, s>>>(keys, vals, n_edges, cursor, adj);
+    if (n_edges) {
+        scatter_keys<<<grid, 256, 0, s>>>(keys, vals, n_edges, cursor, adj);
+        io->launches++;
+    }
     if (n_keys) {
         sort_segments_warp<<<n_sm * 8, 256, 0, s>>>(ptr, n_keys, adj);
         sort_segments_block<<<n_sm * 4, 256, 0, s>>>(ptr, n_keys, adj);
-        if (n_bitmaps) sort_segments_bitmap<<<n_bitmaps, 512, 0, s>>>(ptr, n_keys, adj, max_val, bitmaps);
+        io->launches += 2;
+        if (n_bitmaps) {
+            sort_segments_bitmap<<<n_bitmaps, 512, 0, s>>>(ptr, n_keys, adj, max_val, bitmaps);
+            io->launches++;
+        }
     }
     return cudaGetLastError();
 }
@@ -313,7 +324,7 @@ static void compute_ranks(const mbe_graph* g, bool swapped, std::vector<uint32_t
     while (*n_isolated < nR && deg_by_rank[*n_isolated] == 0) (*n_isolated)++;
 }
 
-mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out) {
+mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out, IoCounters* io) {
     DeviceGraph d;
     d.swapped = g->n_rows > g->n_cols ? 1u : 0u;
     d.nR = d.swapped ? g->n_cols : g->n_rows;
@@ -379,6 +390,7 @@ mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, Devi
         n_big = (uint32_t)n_sm * 2;
         GD_TRY(cudaMalloc(&bitmaps, (size_t)n_big * ((nmax + 31) / 32) * 4));
     }
+    io->h2d += n_rp * 8 + n_e * 4 + (size_t)d.nR * 8;
     GD_TRY(cudaMemcpyAsync(d_row_ptr, sp, n_rp * 8, cudaMemcpyHostToDevice, s));
     if (n_e) GD_TRY(cudaMemcpyAsync(d_col, sp + n_rp * 8, n_e * 4, cudaMemcpyHostToDevice, s));
     if (d.nR) {
@@ -389,13 +401,15 @@ mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, Devi
     if (n_e) {
         expand_edges<<<n_sm * 8, 256, 0, s>>>(d_row_ptr, d_col, g->n_rows, n_e, d_rank_of, (int)d.swapped, e_rank,
                                               e_l);
+        io->launches++;
         GD_TRY(cudaGetLastError());
     }
-    GD_TRY(build_csr(d.nR, n_e, e_rank, e_l, d.r_ptr, d.r_adj, cursor, scan_tmp, d.nL, bitmaps, n_big, n_sm, s));
-    GD_TRY(build_csr(d.nL, n_e, e_l, e_rank, d.l_ptr, d.l_adj, cursor, scan_tmp, d.nR, bitmaps, n_big, n_sm, s));
+    GD_TRY(build_csr(d.nR, n_e, e_rank, e_l, d.r_ptr, d.r_adj, cursor, scan_tmp, d.nL, bitmaps, n_big, n_sm, s, io));
+    GD_TRY(build_csr(d.nL, n_e, e_l, e_rank, d.l_ptr, d.l_adj, cursor, scan_tmp, d.nR, bitmaps, n_big, n_sm, s, io));
     uint32_t nh = std::max(d.nR, d.nL);
     if (nh) {
         elem_hashes<<<(nh + 255) / 256, 256, 0, s>>>(d.nR, d.nL, d.r_orig, (int)d.swapped, d.eR, d.eL);
+        io->launches++;
         GD_TRY(cudaGetLastError());
     }
     GD_TRY(cudaStreamSynchronize(s));

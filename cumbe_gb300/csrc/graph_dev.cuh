@@ -48,6 +48,6 @@ inline GraphView view_of(const DeviceGraph& d) {
     return GraphView{d.nR, d.nL, d.swapped, 0, d.r_ptr, d.r_adj, d.l_ptr, d.l_adj, d.r_orig, d.eR, d.eL};
 }
 
-mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out);
+mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out, IoCounters* io);
 
 }  // namespace mbe

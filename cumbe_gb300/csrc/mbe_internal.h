@@ -19,6 +19,13 @@ struct mbe_graph {
 
 namespace mbe {
 
+// Per-context accounting of what crossed the host/device boundary.
+struct IoCounters {
+    uint64_t launches = 0;   // kernels of this library launched
+    uint64_t h2d = 0;        // bytes copied host -> device
+    uint64_t d2h = 0;        // bytes copied device -> host
+};
+
 // Thread-local error message plumbing.
 mbe_status fail(mbe_status st, const std::string& msg);
 void clear_error();

@@ -129,7 +129,9 @@ typedef struct mbe_result {
     uint64_t count;              /* maximal bicliques (thresholds applied)  */
     uint64_t hash;               /* sum over bicliques of mbe_biclique_hash */
     uint64_t nodes;              /* search-tree nodes evaluated             */
-    uint64_t words;              /* 32-bit words of set data streamed       */
+    uint64_t words;              /* 32-bit words of set data streamed by
+                                    the DFS kernel                          */
+    uint64_t words_expand;       /* words streamed by the root expansion    */
     uint64_t emitted;            /* bicliques written to emit buffers       */
     float ms;                    /* device time of the enumeration kernels  */
     float ms_prep;               /* device time of the root expansion       */
@@ -207,6 +209,10 @@ MBE_API const char* mbe_variant_name(mbe_variant v);
 /* Maps a CLI algorithm string to a variant; unknown strings map to
  * MBE_CUMBE as src/main.cu:122 does. */
 MBE_API mbe_variant mbe_variant_from_name(const char* name);
+
+/* Cumulative accounting of ctx since creation: kernels of this library
+ * launched, bytes copied host->device and device->host. */
+MBE_API mbe_status mbe_ctx_counters(mbe_ctx* ctx, uint64_t* launches, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
 
 /* Launch geometry of the last enumeration on ctx (the CLI's grid_size line). */
 MBE_API mbe_status mbe_ctx_last_grid(mbe_ctx* ctx, uint32_t* grid_expand, uint32_t* grid_dfs, uint32_t* block);

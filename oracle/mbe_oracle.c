@@ -162,6 +162,8 @@ typedef struct {
     int variant;
     uint32_t min_rows, min_cols;
     int k_lo;                 /* only roots with ori_P index >= k_lo      */
+    int stride;               /* only every stride-th root (1 = all)       */
+    int last;                 /* index of the first root in processing order */
     oracle_emit* emit;
     /* per-thread ("per-block") state, src/main.cu:72-86 */
     int *u2L, *L, *v2P, *P, *v2Q, *Q, *R, *x, *L_lp, *R_lp, *P_lp, *Q_lp, *pre_min;
@@ -363,6 +365,10 @@ static void* run_block(void* arg) {
                 int before = s->P_lp[0];
                 int k = atomic_fetch_sub(s->P_ptr, 1);
                 if (k < s->k_lo) k = -1;
+                /* a stride sample skips roots but keeps their Q semantics:
+                 * the next processed root adds every skipped root to Q */
+                while (k >= 0 && s->stride > 1 && (s->last - k) % s->stride != 0) k = atomic_fetch_sub(s->P_ptr, 1);
+                if (k < s->k_lo) k = -1;
                 s->P_lp[0] = k;
                 if (k < 0) break;
                 /* Q gains the roots skipped since this block's previous root (:135-150) */
@@ -481,9 +487,31 @@ static void free_state(ostate* s) {
  * root_lo/root_hi (fractions in [0,1] of the non-isolated roots, taken
  * from the processing tail) bound a sample; 0/1 runs everything.  Returns
  * 0 on success, -1 on allocation failure, -2 on emit overflow. */
+static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr, const uint32_t* col_idx,
+                              int variant, int n_threads, uint32_t min_rows, uint32_t min_cols, double root_frac,
+                              int stride, oracle_result* out, oracle_emit* emit);
+
 ORACLE_API int oracle_ref_enumerate(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr,
                                     const uint32_t* col_idx, int variant, int n_threads, uint32_t min_rows,
                                     uint32_t min_cols, double root_frac, oracle_result* out, oracle_emit* emit) {
+    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, min_rows, min_cols, root_frac, 1,
+                              out, emit);
+}
+
+/* Bounded sample for timing: only every stride-th root in processing
+ * order is expanded (with the full Q of everything processed before it),
+ * so the sample spans all degrees.  The count is that of the sampled
+ * roots' subtrees. */
+ORACLE_API int oracle_ref_enumerate_sampled(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr,
+                                            const uint32_t* col_idx, int variant, int n_threads, int stride,
+                                            oracle_result* out) {
+    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, 0, 0, 0.0,
+                              stride < 1 ? 1 : stride, out, NULL);
+}
+
+static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr, const uint32_t* col_idx,
+                              int variant, int n_threads, uint32_t min_rows, uint32_t min_cols, double root_frac,
+                              int stride, oracle_result* out, oracle_emit* emit) {
     memset(out, 0, sizeof *out);
     ograph g;
     ograph_build(&g, n_rows, n_cols, row_ptr, col_idx);
@@ -518,6 +546,8 @@ ORACLE_API int oracle_ref_enumerate(uint32_t n_rows, uint32_t n_cols, const uint
         st[t].min_rows = min_rows;
         st[t].min_cols = min_cols;
         st[t].k_lo = k_lo;
+        st[t].stride = stride;
+        st[t].last = last;
         st[t].emit = emit;
         if (alloc_state(&st[t], g.nR, g.nL)) rc = -1;
     }

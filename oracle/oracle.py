@@ -66,6 +66,9 @@ def lib():
                                            ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
                                            ctypes.POINTER(_Result), ctypes.POINTER(_Emit)]
         L.oracle_ref_enumerate.restype = ctypes.c_int
+        L.oracle_ref_enumerate_sampled.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u64p, u32p, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Result)]
+        L.oracle_ref_enumerate_sampled.restype = ctypes.c_int
         L.oracle_brute.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u64p, u32p, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.POINTER(_Result), ctypes.POINTER(_Emit)]
         L.oracle_brute.restype = ctypes.c_int
@@ -119,6 +122,17 @@ def ref_enumerate(n_rows, n_cols, row_ptr, col_idx, variant="cuMBE", threads=1, 
     if em:
         out.bicliques = _decode(em, offs, nrows, ids)
     return out
+
+
+def ref_enumerate_sampled(n_rows, n_cols, row_ptr, col_idx, stride, variant="cuMBE", threads=1) -> OracleResult:
+    """The restatement over every stride-th root only (a bounded timing sample)."""
+    rp, ci, prp, pci = _ptrs(row_ptr, col_idx)
+    res = _Result()
+    rc = lib().oracle_ref_enumerate_sampled(n_rows, n_cols, prp, pci, VARIANTS[variant], threads, stride,
+                                            ctypes.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"oracle_ref_enumerate_sampled failed rc={rc}")
+    return OracleResult(res.count, res.hash, res.nodes, res.scanned)
 
 
 def brute(n_rows, n_cols, row_ptr, col_idx, min_rows=0, min_cols=0, emit_cap=0) -> OracleResult:
