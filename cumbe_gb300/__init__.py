@@ -91,6 +91,8 @@ SIGNATURES = {
     "mbe_variant_from_name": (ctypes.c_int, [ctypes.c_char_p]),
     "mbe_ctx_last_grid": (ctypes.c_int, [_VP, _U32P, _U32P, _U32P]),
     "mbe_ctx_counters": (ctypes.c_int, [_VP, _U64P, _U64P, _U64P]),
+    "mbe_enumerate_static": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, _VP, _VP, _VP, _VP, ctypes.c_int,
+                                            _VP, _VP]),
 }
 
 _lib = None

@@ -1331,4 +1331,16 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     return MBE_OK;
 }
 
+// Launchers for callers outside this file that lay out EngineArgs
+// themselves (the static-scratch entry point in capi_static.cu).
+cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s) {
+    expand_roots_kernel<<<grid, kThreadsA, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dfs(const EngineArgs& a, unsigned grid, cudaStream_t s) {
+    dfs_kernel<<<grid, kThreadsB, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 }  // namespace mbe

@@ -50,4 +50,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                       const std::vector<const DeviceGraph*>& graphs, const std::vector<uint2>& roots,
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io);
 
+// Raw launchers of the two enumeration kernels (256 threads per block;
+// dfs_kernel runs 8 warps per block).
+cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s);
+cudaError_t launch_dfs(const EngineArgs& a, unsigned grid, cudaStream_t s);
+
 }  // namespace mbe

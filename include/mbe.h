@@ -210,6 +210,36 @@ MBE_API const char* mbe_variant_name(mbe_variant v);
  * MBE_CUMBE as src/main.cu:122 does. */
 MBE_API mbe_variant mbe_variant_from_name(const char* name);
 
+/* ---- allocation-free enumeration --------------------------------------- */
+
+/* Working memory of mbe_enumerate_static: one array compiled into the
+ * library, held on every GPU that loads it until the process exits. */
+#define MBE_STATIC_SCRATCH_BYTES (64u << 20)
+/* Largest side mbe_enumerate_static accepts. */
+#define MBE_STATIC_MAX_VERTICES 4096u
+
+/* Counts and hashes the maximal bicliques of a small graph without
+ * allocating any device memory.  No counterpart in the reference: it is for
+ * callers that may not allocate device memory while they run (hosts that
+ * own the device through their own pool allocator, latency-bound serving
+ * loops, plugin runtimes without an allocation budget).  The caller passes
+ * the graph as two sorted, duplicate-free device CSRs with 32-bit offsets,
+ * d_row_ptr[n_rows+1]/d_row_idx (rows -> cols) and its transpose
+ * d_col_ptr[n_cols+1]/d_col_idx (cols -> rows), and a device buffer
+ * d_result[2] that receives {count, hash} in stream order.  All working
+ * memory comes from a fixed 64 MiB array inside the library: no cudaMalloc
+ * or cudaFree is called.  Limits: at most MBE_STATIC_MAX_VERTICES per side
+ * (MBE_ERR_CAPACITY beyond), and the search must fit the array
+ * (MBE_ERR_OUT_OF_MEMORY otherwise).  The first call on a device, with that
+ * device current, looks the array's address up; make it before any stream
+ * capture.  The call synchronises `stream` to read the device status.
+ * Every call reuses the same array: calls that overlap on the GPU race, so
+ * serialise them.  `stream` is a cudaStream_t (NULL = default stream). */
+MBE_API mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, const uint32_t* d_row_ptr,
+                                        const uint32_t* d_row_idx, const uint32_t* d_col_ptr,
+                                        const uint32_t* d_col_idx, mbe_variant variant, uint64_t* d_result,
+                                        void* stream);
+
 /* Cumulative accounting of ctx since creation: kernels of this library
  * launched, bytes copied host->device and device->host. */
 MBE_API mbe_status mbe_ctx_counters(mbe_ctx* ctx, uint64_t* launches, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
