@@ -1,0 +1,61 @@
+"""Golden fixtures (tests/golden): committed .bi graphs with the oracle's
+expected count and canonical hash, and the counts the reference's own
+kernels printed for them (reference_counts.json, made by
+tests/golden/ref_counts.py on a GPU)."""
+import json
+import os
+
+import pytest
+
+import cumbe_gb300 as cm
+import oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+EXPECTED = json.load(open(os.path.join(GOLD, "expected.json")))
+REF_PATH = os.path.join(GOLD, "reference_counts.json")
+REFERENCE = json.load(open(REF_PATH)) if os.path.exists(REF_PATH) else {}
+NAMES = sorted(EXPECTED)
+
+
+def _load(name):
+    return cm.Graph.load_bi(os.path.join(GOLD, EXPECTED[name]["file"]))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_fixture(built, name):
+    nr, nc, rp, ci = _load(name).csr()
+    r = oracle.ref_enumerate(nr, nc, rp, ci, threads=4)
+    assert r.count == EXPECTED[name]["count"]
+    assert f"{r.hash:#018x}" == EXPECTED[name]["hash"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_reference_kernels_agree_with_oracle(name):
+    """The pin.  The oracle restates the reference's phase-1 search, which
+    is the whole of its noWS kernel: that kernel printed the oracle's count
+    on every fixture (the reference counts in int32).  All four reference
+    variants agree on the power-law fixtures.  On small random fixtures the
+    reference's work-stealing variants (cuMBE, noRS, noES) can undercount:
+    their counts are recorded and must never exceed the oracle's."""
+    if name not in REFERENCE:
+        pytest.skip("no reference run recorded for this fixture")
+    want = EXPECTED[name]["count"] % 2**32
+    rec = REFERENCE[name]
+    assert rec["noWS"]["count"] % 2**32 == want
+    for variant in ("cuMBE", "noRS", "noES"):
+        got = rec[variant]["count"] % 2**32
+        if name.startswith("power_law"):
+            assert got == want, variant
+        else:
+            assert got <= want, variant
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_matches_fixture(engine, name):
+    g = _load(name)
+    for variant in ["cuMBE", "noRS", "noES", "noWS"]:
+        r = engine.enumerate(g, variant)
+        assert r.count == EXPECTED[name]["count"], variant
+        assert f"{r.hash:#018x}" == EXPECTED[name]["hash"], variant
