@@ -28,11 +28,13 @@ def nvcc() -> str:
     return cand
 
 
-def _flags(debug: bool = False) -> list[str]:
+def _flags() -> list[str]:
     f = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-    if debug:
-        f += ["-DMBE_DEBUG"]
+    # MBE_PROFILE=1 compiles the per-section cycle counters of dfs_kernel in
+    # (printed to stderr after each enumeration); off by default.
+    if os.environ.get("MBE_PROFILE") == "1":
+        f += ["-DMBE_PROFILE"]
     return f
 
 

@@ -18,6 +18,7 @@
 //     generalised to any depth).  Termination is an outstanding-task
 //     counter, not a grid barrier; every wait is bounded by %globaltimer.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -77,6 +78,14 @@ __device__ bool push_task(const EngineArgs& a, Task t) {
     atomicExch(&a.ready[slot], tk + 1u);
     return true;
 }
+
+#ifdef MBE_PROFILE
+#define PROF_T0() long long prof_t0__ = clock64()
+#define PROF_ADD(acc_arr, sec) do { (acc_arr)[2 * (sec)] += clock64() - prof_t0__; (acc_arr)[2 * (sec) + 1]++; prof_t0__ = clock64(); } while (0)
+#else
+#define PROF_T0() do {} while (0)
+#define PROF_ADD(acc_arr, sec) do {} while (0)
+#endif
 
 // Bump allocation from the node pool; ~0 when it does not fit.  Sizes are
 // rounded to 128-byte lines so that records written by one SM and read by
@@ -360,6 +369,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                     h->sR = G.eR[x] + s_sabs;
                     h->words = (uint32_t)rw;
                     h->rlist = 0;
+                    h->flags = 0;
                 }
                 for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
                     wmap[w] = w;
@@ -539,6 +549,12 @@ struct WarpCtx {
     unsigned long long* scrKeysQ;
     uint32_t* sLi;
     uint32_t* sNz;
+    uint32_t* scrPack;     // 5 x kc words: qrow, qpos, srow, spos, porder
+    uint32_t* sBucket;     // 32 words of shared memory
+#ifdef MBE_PROFILE
+    long long prof[kProfSlots];
+    unsigned long long last_busy;  // globaltimer when the warp last finished a task
+#endif
 };
 
 // Ticket queue: an idle warp takes the next slot index with one atomicAdd
@@ -547,7 +563,7 @@ struct WarpCtx {
 // ends when the slot is ready, or when pending == 0 (no queued and no
 // running task: nothing can be pushed any more), or on an error, or when
 // no warp has made progress for timeout_ns.
-__device__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my_path) {
+__device__ __noinline__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my_path) {
     unsigned lane = lane_id();
     int state = 0;  // 1 = got, 2 = done
     uint32_t h = 0;
@@ -617,31 +633,323 @@ __device__ __forceinline__ bool row_subset(const uint32_t* M, uint32_t n, const 
     return true;
 }
 
+struct RecView {
+    uint32_t W, n, nq, flags;
+    const uint32_t* map;   // wmap[W], or lmap[32] when packed
+    const uint32_t* Lm;
+    const uint32_t* cand;
+    const uint32_t* cnt;
+    const uint32_t* M;
+};
+
+__device__ __forceinline__ RecView rec_view(const uint32_t* nd) {
+    const NodeHdr* h = (const NodeHdr*)nd;
+    RecView v;
+    v.W = h->W;
+    v.n = h->n;
+    v.nq = h->nq;
+    v.flags = h->flags;
+    v.map = nd + kHdrWords;
+    v.Lm = v.map + ((v.flags & kRecPacked) ? 32u : pad4(v.W));
+    v.cand = v.Lm + pad4(v.W);
+    v.cnt = v.cand + pad4(v.n);
+    v.M = v.cnt + pad4(v.n);
+    return v;
+}
+
+// bits of x selected by m, packed to the low end in order
+__device__ __forceinline__ uint32_t pext32(uint32_t x, uint32_t m) {
+    uint32_t r = 0, bit = 1;
+    while (m) {
+        uint32_t low = m & (0u - m);
+        if (x & low) r |= bit;
+        bit <<= 1;
+        m &= m - 1;
+    }
+    return r;
+}
+
+// Stable counting sort by a small key (< 32) within a warp: keys are
+// produced by key_of(i) for items 0..n-1 in order; the item index of every
+// output position is written to out[].  Buckets live in shared memory; items
+// with equal keys keep their input order.
+template <typename KeyOf>
+__device__ void warp_bucket_sort(uint32_t n, KeyOf key_of, uint32_t* out, uint32_t* sb) {
+    const unsigned lane = lane_id();
+    sb[lane] = 0;
+    __syncwarp();
+    for (uint32_t base = 0; base < n; base += 32) {
+        uint32_t i = base + lane;
+        bool v = i < n;
+        uint32_t key = v ? key_of(i) : 32u;
+        unsigned grp = __match_any_sync(kFull, key);
+        if (v && (grp & lanemask_lt()) == 0) atomicAdd(&sb[key], __popc(grp));
+    }
+    __syncwarp();
+    uint32_t cnt = sb[lane], ex = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, ex, o);
+        if (lane >= (unsigned)o) ex += y;
+    }
+    __syncwarp();
+    sb[lane] = ex - cnt;  // exclusive offsets
+    __syncwarp();
+    for (uint32_t base = 0; base < n; base += 32) {
+        uint32_t i = base + lane;
+        bool v = i < n;
+        uint32_t key = v ? key_of(i) : 32u;
+        unsigned grp = __match_any_sync(kFull, key);
+        uint32_t off = v ? sb[key] : 0u;
+        if (v) out[off + __popc(grp & lanemask_lt())] = i;
+        __syncwarp();
+        if (v && (grp & lanemask_lt()) == 0) sb[key] = off + __popc(grp);
+        __syncwarp();
+    }
+}
+
+// Bit compress with a fixed mask (Warren, Hacker's Delight, 2nd ed., 7-4):
+// the five shift masks depend on the mask only, so a build that packs many
+// rows against the same L_i computes them once and then packs each row in
+// five shift/mask steps.
+struct CompressPlan {
+    uint32_t mask, mv[5];
+};
+
+__device__ __forceinline__ CompressPlan compress_plan(uint32_t m) {
+    CompressPlan p;
+    p.mask = m;
+    uint32_t mk = ~m << 1;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        uint32_t mp = mk ^ (mk << 1);
+        mp ^= mp << 2;
+        mp ^= mp << 4;
+        mp ^= mp << 8;
+        mp ^= mp << 16;
+        uint32_t mv = mp & m;
+        p.mv[i] = mv;
+        m = (m ^ mv) | (mv >> (1u << i));
+        mk &= ~mp;
+    }
+    return p;
+}
+
+__device__ __forceinline__ uint32_t compress32(uint32_t x, const CompressPlan& p) {
+    x &= p.mask;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        uint32_t t = x & p.mv[i];
+        x = (x ^ t) | (t >> (1u << i));
+    }
+    return x;
+}
+
+// L_i-restricted row of candidate c, packed to one word (|L_i| <= 32);
+// plan0 is the compress plan of Li[0], used when L_i spans one word.
+__device__ __forceinline__ uint32_t packed_row(const uint32_t* M, uint32_t n, const uint32_t* Nz,
+                                               const uint32_t* Li, uint32_t nnz, uint32_t c,
+                                               const CompressPlan& plan0) {
+    if (nnz == 1) return compress32(M[(size_t)Nz[0] * n + c], plan0);
+    uint32_t row = 0, sh = 0;
+    for (uint32_t k = 0; k < nnz; k++) {
+        row |= pext32(M[(size_t)Nz[k] * n + c], Li[k]) << sh;
+        sh += __popc(Li[k]);
+    }
+    return row;
+}
+
+// Child record construction when |L_i| <= 32: rows are packed to one word
+// first, so ordering is a counting sort over at most 31 counts and the Q
+// reduction compares single words held in lane registers.  Produces the
+// same record (same order, same reduction) as the general path would with
+// packed rows.
+__device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const NodeHdr* h, uint32_t xi, uint32_t li,
+                                 uint32_t nnz, const uint32_t* Li, const uint32_t* Nz, uint32_t npp, uint32_t nR2,
+                                 unsigned long long sR2, WarpCtx& wc, ResultAcc& acc) {
+    const unsigned lane = lane_id();
+    const uint32_t n = R.n, nq = R.nq;
+    const uint32_t* M = R.M;
+    const uint32_t kc = a.scr_kc;
+    uint32_t* qrow = wc.scrPack;
+    uint32_t* qpos = qrow + kc;
+    uint32_t* srow = qpos + kc;
+    uint32_t* spos = srow + kc;
+    uint32_t* porder = spos + kc;
+    const CompressPlan plan0 = compress_plan(Li[0]);
+    ChildOut out{nullptr, 0, 0};
+    // Q' = rows of Q u P[0..i) meeting L_i, packed, in parent order
+    uint32_t m = 0;
+    for (uint32_t base = 0; base < xi; base += 64) {  // two chunks per step: independent loads
+        uint32_t c0 = base + lane, c1 = base + 32 + lane;
+        uint32_t r0 = c0 < xi ? packed_row(M, n, Nz, Li, nnz, c0, plan0) : 0u;
+        uint32_t r1 = c1 < xi ? packed_row(M, n, Nz, Li, nnz, c1, plan0) : 0u;
+        unsigned b0 = __ballot_sync(kFull, r0 != 0), b1 = __ballot_sync(kFull, r1 != 0);
+        if (r0) {
+            uint32_t p = m + __popc(b0 & lanemask_lt());
+            qrow[p] = r0;
+            qpos[p] = c0;
+        }
+        m += __popc(b0);
+        if (r1) {
+            uint32_t p = m + __popc(b1 & lanemask_lt());
+            qrow[p] = r1;
+            qpos[p] = c1;
+        }
+        m += __popc(b1);
+    }
+    __syncwarp();
+    acc.words += (unsigned long long)xi * nnz;
+    // count descending (key li - count in 1..31), parent order within a count
+    warp_bucket_sort(m, [&](uint32_t i) { return li - __popc(qrow[i]); }, porder, wc.sBucket);
+    __syncwarp();
+    for (uint32_t t = lane; t < m; t += 32) {
+        uint32_t i = porder[t];
+        srow[t] = qrow[i];
+        spos[t] = qpos[i];
+    }
+    __syncwarp();
+    // reduction, 32 candidates per step: every lane tests its row against the
+    // window (the first kKeepWindow kept rows, in lane registers); the
+    // survivors are then taken in order, and each one that joins the window
+    // is tested against by all later lanes at once.  Same result as the
+    // one-by-one greedy.
+    uint32_t kept_row = 0, nk = 0, nq2 = 0;
+    for (uint32_t base = 0; base < m; base += 32) {
+        uint32_t idx = base + lane;
+        bool valid = idx < m;
+        uint32_t r = valid ? srow[idx] : 0u, p = valid ? spos[idx] : 0u;
+        bool dom = !valid;
+        for (uint32_t j = 0; j < nk; j++) {
+            uint32_t kr = __shfl_sync(kFull, kept_row, j);
+            dom = dom || (r & ~kr) == 0;
+        }
+        unsigned pending = __ballot_sync(kFull, !dom), keep = 0;
+        while (pending) {
+            uint32_t j = __ffs(pending) - 1;
+            pending &= pending - 1;
+            keep |= 1u << j;
+            if (nk < kKeepWindow) {
+                uint32_t rj = __shfl_sync(kFull, r, j);
+                if (lane == nk) kept_row = rj;
+                nk++;
+                pending &= ~__ballot_sync(kFull, lane > j && (r & ~rj) == 0);
+            }
+        }
+        __syncwarp();  // all reads of this chunk precede the compacting writes
+        if ((keep >> lane) & 1u) {
+            uint32_t q = nq2 + __popc(keep & lanemask_lt());
+            srow[q] = r;
+            spos[q] = p;
+        }
+        nq2 += __popc(keep);
+        __syncwarp();
+    }
+    // P' by count ascending, parent order within a count (keys in scan order)
+    warp_bucket_sort(npp, [&](uint32_t t) { return (uint32_t)(wc.scrKeysP[t] >> 32); }, porder, wc.sBucket);
+    __syncwarp();
+    // allocate and write
+    const uint32_t n2 = nq2 + npp;
+    const uint64_t rw = record_words(1, n2, true);
+    uint32_t* rec;
+    if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
+        rec = wc.arena + wc.arena_top;
+        out.size = (uint32_t)rw;
+    } else {
+        unsigned long long off = 0;
+        if (lane == 0) {
+            off = pool_alloc(a, rw);
+            if (off == ~0ull) set_error(a, kErrPool, rw);
+        }
+        off = __shfl_sync(kFull, off, 0);
+        if (off == ~0ull) return out;
+        rec = a.pool + off;
+        out.size = 0;
+    }
+    uint32_t* map2 = rec + kHdrWords;
+    uint32_t* Lm2 = map2 + 32;
+    uint32_t* cand2 = Lm2 + 4;
+    uint32_t* cnt2 = cand2 + pad4(n2);
+    uint32_t* M2 = cnt2 + pad4(n2);
+    if (lane == 0) {
+        NodeHdr* h2 = (NodeHdr*)rec;
+        h2->graph = h->graph;
+        h2->root = h->root;
+        h2->W = 1;
+        h2->n = n2;
+        h2->nq = nq2;
+        h2->l = li;
+        h2->nRset = nR2;
+        h2->depth = h->depth + 1;
+        h2->sR = sR2;
+        h2->words = (uint32_t)rw;
+        h2->rlist = 0;
+        h2->flags = kRecPacked;
+        Lm2[0] = li == 32 ? 0xFFFFFFFFu : ((1u << li) - 1u);
+    }
+    // lane t < li: root bit of the t-th set bit of L_i (words in order)
+    if (lane < li) {
+        const bool parent_packed = (R.flags & kRecPacked) != 0;
+        uint32_t before = 0, rootbit = 0;
+        for (uint32_t k = 0; k < nnz; k++) {
+            uint32_t c = __popc(Li[k]);
+            if (lane < before + c) {
+                uint32_t bits = Li[k];
+                for (uint32_t s = before; s < lane; s++) bits &= bits - 1;
+                uint32_t b = __ffs(bits) - 1;
+                rootbit = parent_packed ? R.map[b] : R.map[Nz[k]] * 32 + b;
+                break;
+            }
+            before += c;
+        }
+        map2[lane] = rootbit;
+    }
+    for (uint32_t t = lane; t < nq2; t += 32) {
+        cand2[t] = R.cand[spos[t]];
+        cnt2[t] = 0;
+        M2[t] = srow[t];
+    }
+    for (uint32_t t = lane; t < npp; t += 32) {
+        unsigned long long key = wc.scrKeysP[porder[t]];
+        uint32_t c = nq + (uint32_t)key;
+        cand2[nq2 + t] = R.cand[c];
+        cnt2[nq2 + t] = (uint32_t)(key >> 32);
+        M2[nq2 + t] = packed_row(M, n, Nz, Li, nnz, c, plan0);
+    }
+    acc.words += (unsigned long long)n2 + (unsigned long long)npp * nnz;
+    __syncwarp();
+    out.rec = rec;
+    out.nchild = npp;
+    return out;
+}
+
 // Evaluates child i of the node record `nd` (one tree node).  Counts and
 // hashes the biclique when maximal; materialises the child record when it
-// has candidates.  Warp-collective.
+// has candidates.  Warp-collective.  known_max: the caller has already
+// established that no row of Q u P[0..i) covers L_i (batch prefilter).
 //
 // The child's Q part is ordered by |N(v) n L_i| descending and reduced:
 // a Q row contained in one of the first kKeepWindow kept rows is dropped,
 // since whatever it covers in the subtree the containing row covers too.
 // Large rows first make the first covering row of a non-maximal
-// descendant appear within the first few candidates.
+// descendant appear within the first few candidates.  A child with
+// |L_i| <= 32 is written packed: one word per row, L bits dense.
 __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, WarpCtx& wc,
-                               ResultAcc& acc_out, bool replay) {
+                               ResultAcc& acc_out, bool replay, bool known_max) {
     // a replayed evaluation re-derives a donated node: its counts belong to
     // the donor and are discarded
     ResultAcc scratch_acc{};
     ResultAcc& acc = replay ? scratch_acc : acc_out;
     const unsigned lane = lane_id();
+    PROF_T0();
     const NodeHdr* h = (const NodeHdr*)nd;
-    const uint32_t W = h->W, n = h->n, nq = h->nq;
-    const uint32_t* wmap = nd + kHdrWords;
-    const uint32_t* Lm = wmap + pad4(W);
-    const uint32_t* cand = Lm + pad4(W);
-    const uint32_t* cntv = cand + pad4(n);
-    const uint32_t* M = cntv + pad4(n);
+    const RecView R = rec_view(nd);
+    const uint32_t W = R.W, n = R.n, nq = R.nq;
+    const bool packed = (R.flags & kRecPacked) != 0;
+    const uint32_t* M = R.M;
+    const uint32_t* cand = R.cand;
     const uint32_t xi = nq + i;
-    const uint32_t li = cntv[xi];
+    const uint32_t li = R.cnt[xi];
     uint32_t* Li = W <= kSmemW ? wc.sLi : wc.scrLi;
     uint32_t* Nz = W <= kSmemW ? wc.sNz : wc.scrNz;
     ChildOut out{nullptr, 0, 0};
@@ -650,7 +958,7 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
     uint32_t nnz = 0;
     for (uint32_t base = 0; base < W; base += 32) {
         uint32_t w = base + lane;
-        uint32_t v = w < W ? (Lm[w] & M[(size_t)w * n + xi]) : 0u;
+        uint32_t v = w < W ? (R.Lm[w] & M[(size_t)w * n + xi]) : 0u;
         unsigned bal = __ballot_sync(kFull, v != 0);
         if (v) {
             uint32_t pos = nnz + __popc(bal & lanemask_lt());
@@ -660,46 +968,59 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         nnz += __popc(bal);
     }
     __syncwarp();
-    acc.nodes++;
+    if (!known_max) acc.nodes++;
     acc.words += W;
 
     // 2. maximality against Q u P[0..i); counts kept for Q'
-    const bool es = a.variant != MBE_NOES;
-    bool maximal = true;
-    for (uint32_t base = 0; base < xi; base += 32) {
-        uint32_t c = base + lane;
-        uint32_t cc = 0;
-        if (c < xi) {
-            for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
-            wc.scrQcnt[c] = cc;
+    if (!known_max) {
+        const bool es = a.variant != MBE_NOES;
+        bool maximal = true;
+        for (uint32_t base = 0; base < xi; base += 32) {
+            uint32_t c = base + lane;
+            uint32_t cc = 0;
+            if (c < xi) {
+                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+                wc.scrQcnt[c] = cc;
+            }
+            unsigned full = __ballot_sync(kFull, c < xi && cc == li);
+            acc.words += (unsigned long long)nnz * min(32u, xi - base);
+            if (full) {
+                maximal = false;
+                if (es) break;
+            }
         }
-        unsigned full = __ballot_sync(kFull, c < xi && cc == li);
-        acc.words += (unsigned long long)nnz * min(32u, xi - base);
-        if (full) {
-            maximal = false;
-            if (es) break;
-        }
+        __syncwarp();
+        PROF_ADD(wc.prof, kProfQscan);
+        if (!maximal) return out;
     }
-    __syncwarp();
-    if (!maximal) return out;
 
-    // 3. expansion over P(i..]
+    // 3. expansion over P(i..], two chunks per step (independent loads)
     uint32_t npp = 0, nabs = 0;
     unsigned long long sabs = 0;
-    for (uint32_t base = xi + 1; base < n; base += 32) {
-        uint32_t c = base + lane;
-        bool valid = c < n;
-        uint32_t cc = 0;
-        if (valid)
-            for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
-        bool absorbed = valid && cc == li;
-        bool partial = valid && cc > 0 && cc < li;
-        if (absorbed) sabs += G.eR[cand[c]];
-        unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
-        if (partial) wc.scrKeysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
-        npp += __popc(pb);
-        nabs += __popc(ab);
-        acc.words += (unsigned long long)nnz * min(32u, n - base);
+    for (uint32_t base = xi + 1; base < n; base += 64) {
+        uint32_t cc2[2];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; h2++) {
+            uint32_t c = base + 32 * h2 + lane;
+            uint32_t cc = 0;
+            if (c < n)
+                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+            cc2[h2] = cc;
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < 2; h2++) {
+            uint32_t c = base + 32 * h2 + lane;
+            bool valid = c < n;
+            uint32_t cc = cc2[h2];
+            bool absorbed = valid && cc == li;
+            bool partial = valid && cc > 0 && cc < li;
+            if (absorbed) sabs += G.eR[cand[c]];
+            unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
+            if (partial) wc.scrKeysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
+            npp += __popc(pb);
+            nabs += __popc(ab);
+        }
+        acc.words += (unsigned long long)nnz * min(64u, n - base);
     }
     __syncwarp();
     sabs = warp_sum(sabs);
@@ -710,12 +1031,16 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
     if (li >= a.minL && nR2 >= a.minR) {
         const uint32_t* L0 = G.r_adj + G.r_ptr[h->root];
         unsigned long long sl = 0;
-        for (uint32_t k = lane; k < nnz; k += 32) {
-            uint32_t bits = Li[k], b0 = wmap[Nz[k]] * 32;
-            while (bits) {
-                uint32_t t = __ffs(bits) - 1;
-                bits &= bits - 1;
-                sl += G.eL[L0[b0 + t]];
+        if (packed) {
+            if ((Li[0] >> lane) & 1u) sl = G.eL[L0[R.map[lane]]];
+        } else {
+            for (uint32_t k = lane; k < nnz; k += 32) {
+                uint32_t bits = Li[k], b0 = R.map[Nz[k]] * 32;
+                while (bits) {
+                    uint32_t t = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    sl += G.eL[L0[b0 + t]];
+                }
             }
         }
         sl = warp_sum(sl);
@@ -724,7 +1049,26 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
     }
 
     // 5. child record
+    PROF_ADD(wc.prof, kProfExpand);
     if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
+    if (li <= 32) {
+        out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, wc, acc);
+        PROF_ADD(wc.prof, kProfBuild);
+        return out;
+    }
+    if (known_max) {
+        // the prefilter only settled maximality: count Q u P[0..i) now
+        for (uint32_t base = 0; base < xi; base += 32) {
+            uint32_t c = base + lane;
+            if (c < xi) {
+                uint32_t cc = 0;
+                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+                wc.scrQcnt[c] = cc;
+            }
+        }
+        acc.words += (unsigned long long)nnz * xi;
+        __syncwarp();
+    }
 
     // 5a. Q' = Q u P[0..i) restricted to rows meeting L_i, by count descending
     uint32_t m = 0;
@@ -747,32 +1091,35 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         warp_sort_u64(wc.scrKeysQ, N);
     }
     __syncwarp();
-    // 5b. reduction: greedy prefix until kKeepWindow rows are kept, then every
-    // remaining row is tested against those rows in parallel
-    uint32_t kept_c = 0, nk = 0, pos = 0;  // lane j holds the j-th kept candidate
-    while (pos < m && nk < kKeepWindow) {
-        uint32_t c = (uint32_t)wc.scrKeysQ[pos];
-        bool dom = lane < nk && row_subset(M, n, Nz, Li, nnz, c, kept_c);
-        if (!__any_sync(kFull, dom)) {
-            if (lane == nk) kept_c = c;
-            if (lane == 0) wc.scrKeysQ[nk] = c;  // compacted in place (nk <= pos)
-            nk++;
-        }
-        pos++;
-    }
-    uint32_t nq2 = nk;
-    for (uint32_t base = pos; base < m; base += 32) {
+    // 5b. reduction, 32 candidates per step (same scheme as build_packed):
+    // test against the window of kept rows in parallel, then take the
+    // survivors in order, each row joining the window tested by later lanes
+    uint32_t kept_c = 0, nk = 0, nq2 = 0;  // lane j holds the j-th kept candidate
+    for (uint32_t base = 0; base < m; base += 32) {
         uint32_t idx = base + lane;
-        uint32_t c = idx < m ? (uint32_t)wc.scrKeysQ[idx] : 0u;
-        bool keep = idx < m;
+        bool valid = idx < m;
+        uint32_t c = valid ? (uint32_t)wc.scrKeysQ[idx] : 0u;
+        bool dom = !valid;
         for (uint32_t j = 0; j < nk; j++) {
             uint32_t kc = __shfl_sync(kFull, kept_c, j);
-            if (keep && row_subset(M, n, Nz, Li, nnz, c, kc)) keep = false;
+            if (!dom && row_subset(M, n, Nz, Li, nnz, c, kc)) dom = true;
         }
-        unsigned bal = __ballot_sync(kFull, keep);
+        unsigned pending = __ballot_sync(kFull, !dom), keep = 0;
+        while (pending) {
+            uint32_t j = __ffs(pending) - 1;
+            pending &= pending - 1;
+            keep |= 1u << j;
+            if (nk < kKeepWindow) {
+                uint32_t cj = __shfl_sync(kFull, c, j);
+                if (lane == nk) kept_c = cj;
+                nk++;
+                bool d = ((pending >> lane) & 1u) && row_subset(M, n, Nz, Li, nnz, c, cj);
+                pending &= ~__ballot_sync(kFull, d);
+            }
+        }
         __syncwarp();  // all reads of this chunk precede the compacting writes
-        if (keep) wc.scrKeysQ[nq2 + __popc(bal & lanemask_lt())] = c;
-        nq2 += __popc(bal);
+        if ((keep >> lane) & 1u) wc.scrKeysQ[nq2 + __popc(keep & lanemask_lt())] = c;
+        nq2 += __popc(keep);
         __syncwarp();
     }
     acc.words += (unsigned long long)m * nnz;
@@ -790,8 +1137,9 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
     __syncwarp();
 
     // 5d. allocate and write the record
-    const uint32_t n2 = nq2 + npp, W2 = nnz;
-    const uint64_t rw = record_words(W2, n2);
+    const bool packed2 = li <= 32;
+    const uint32_t n2 = nq2 + npp, W2 = packed2 ? 1u : nnz;
+    const uint64_t rw = record_words(W2, n2, packed2);
     uint32_t* rec;
     if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
         rec = wc.arena + wc.arena_top;
@@ -807,8 +1155,8 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         rec = a.pool + off;
         out.size = 0;
     }
-    uint32_t* wmap2 = rec + kHdrWords;
-    uint32_t* Lm2 = wmap2 + pad4(W2);
+    uint32_t* map2 = rec + kHdrWords;
+    uint32_t* Lm2 = map2 + (packed2 ? 32u : pad4(W2));
     uint32_t* cand2 = Lm2 + pad4(W2);
     uint32_t* cnt2 = cand2 + pad4(n2);
     uint32_t* M2 = cnt2 + pad4(n2);
@@ -825,30 +1173,92 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         h2->sR = sR2;
         h2->words = (uint32_t)rw;
         h2->rlist = 0;
+        h2->flags = packed2 ? kRecPacked : 0u;
     }
-    for (uint32_t k = lane; k < W2; k += 32) {
-        wmap2[k] = wmap[Nz[k]];
-        Lm2[k] = Li[k];
+    if (packed2) {
+        // lane t < li: root bit of the t-th set bit of L_i (words in order)
+        if (lane < li) {
+            uint32_t before = 0, rootbit = 0;
+            for (uint32_t k = 0; k < nnz; k++) {
+                uint32_t c = __popc(Li[k]);
+                if (lane < before + c) {
+                    uint32_t bits = Li[k];
+                    for (uint32_t s = before; s < lane; s++) bits &= bits - 1;
+                    uint32_t b = __ffs(bits) - 1;
+                    rootbit = packed ? R.map[b] : R.map[Nz[k]] * 32 + b;
+                    break;
+                }
+                before += c;
+            }
+            map2[lane] = rootbit;
+        }
+        if (lane == 0) Lm2[0] = li == 32 ? 0xFFFFFFFFu : ((1u << li) - 1u);
+    } else {
+        for (uint32_t k = lane; k < W2; k += 32) {
+            map2[k] = R.map[Nz[k]];
+            Lm2[k] = Li[k];
+        }
     }
-    for (uint32_t t = lane; t < nq2; t += 32) {
-        uint32_t c = (uint32_t)wc.scrKeysQ[t];
+    for (uint32_t t = lane; t < n2; t += 32) {
+        uint32_t c, cntv;
+        if (t < nq2) {
+            c = (uint32_t)wc.scrKeysQ[t];
+            cntv = 0;
+        } else {
+            unsigned long long key = wc.scrKeysP[t - nq2];
+            c = nq + (uint32_t)key;
+            cntv = (uint32_t)(key >> 32);
+        }
         cand2[t] = cand[c];
-        cnt2[t] = 0;
-        for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + t] = M[(size_t)Nz[k] * n + c] & Li[k];
-    }
-    for (uint32_t t = lane; t < npp; t += 32) {
-        unsigned long long key = wc.scrKeysP[t];
-        uint32_t c = nq + (uint32_t)key;
-        uint32_t pos2 = nq2 + t;
-        cand2[pos2] = cand[c];
-        cnt2[pos2] = (uint32_t)(key >> 32);
-        for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + pos2] = M[(size_t)Nz[k] * n + c] & Li[k];
+        cnt2[t] = cntv;
+        if (packed2) {
+            uint32_t row = 0, sh = 0;
+            for (uint32_t k = 0; k < nnz; k++) {
+                row |= pext32(M[(size_t)Nz[k] * n + c], Li[k]) << sh;
+                sh += __popc(Li[k]);
+            }
+            M2[t] = row;
+        } else {
+            for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + t] = M[(size_t)Nz[k] * n + c] & Li[k];
+        }
     }
     acc.words += (unsigned long long)W2 * n2;
     __syncwarp();
+    PROF_ADD(wc.prof, kProfBuild);
     out.rec = rec;
     out.nchild = npp;
     return out;
+}
+
+// Maximality of up to 32 consecutive children of a record with one-word
+// rows, one lane per child: lane j takes child base + j and walks the rows
+// of Q u P[0..i) in order until one covers L_i.  At every step all lanes
+// read the same row (one broadcast load), eight rows per step.  Returns the
+// children no row covers.  Exact: the same test eval_child makes.
+__device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, ResultAcc& acc) {
+    const unsigned lane = lane_id();
+    const bool active = lane < nb;
+    const uint32_t xi = R.nq + base + lane;
+    const uint32_t Li = active ? (R.Lm[0] & R.M[xi]) : 0u;
+    const uint32_t lim = active ? xi : 0u;
+    bool covered = !active;
+    uint32_t c = 0;
+    while (__any_sync(kFull, !covered && c < lim)) {
+#pragma unroll
+        for (uint32_t u = 0; u < 8; u++) {
+            uint32_t cc = c + u;
+            if (!covered && cc < lim) {
+                uint32_t r = R.M[cc];
+                covered = (r & Li) == Li;
+            }
+        }
+        c += 8;
+    }
+    unsigned long long scanned = active ? min(c, lim) : 0u;
+    scanned = warp_sum(scanned);
+    acc.words += scanned + nb;
+    acc.nodes += nb;
+    return __ballot_sync(kFull, active && !covered);
 }
 
 // Gives the upper half of the remaining children of the shallowest frame
@@ -856,7 +1266,7 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
 // is in the node pool is shared by pointer; a frame whose record lives in
 // this warp's arena is described by the child-index path from frame 0
 // (always a pool record), which the receiver replays.  Warp-collective.
-__device__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc) {
+__device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc) {
     unsigned lane = lane_id();
     int k = -1;
     for (int base = 0; base <= depth && k < 0; base += 32) {
@@ -880,7 +1290,7 @@ __device__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCt
     uint32_t* nd = (uint32_t*)fr.node;
     bool in_arena = nd >= wc.arena && nd < wc.arena + a.arena_words;
     // path element j = the child of frame j that frame j+1 expands (k <= kMaxPath <= 31)
-    uint32_t pe = ((int)lane < k) ? frames[lane].next - 1 : 0u;
+    uint32_t pe = ((int)lane < k) ? frames[lane].cur : 0u;
     Task t{};
     t.begin = mid;
     t.end = fr.end;
@@ -894,7 +1304,7 @@ __device__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCt
     __syncwarp();
 }
 
-__device__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
+__device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
     if (lane_id() == 0) {
         ResultAcc* r = &a.results[graph];
         if (acc.count) atomicAdd(&r->count, acc.count);
@@ -905,9 +1315,10 @@ __device__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
     acc = ResultAcc{};
 }
 
-__global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
+__global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
     __shared__ uint32_t sLi[kWarpsB][kSmemW];
     __shared__ uint32_t sNz[kWarpsB][kSmemW];
+    __shared__ uint32_t sBucket[kWarpsB][32];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const size_t gw = (size_t)blockIdx.x * kWarpsB + warp;
     Frame* frames = a.frames + gw * a.max_frames;
@@ -922,14 +1333,28 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
     size_t koff = (2 * (size_t)a.max_W + a.scr_n + 1) & ~(size_t)1;
     wc.scrKeysP = (unsigned long long*)(scr + koff);
     wc.scrKeysQ = wc.scrKeysP + a.scr_kc;
+    wc.scrPack = (uint32_t*)(wc.scrKeysQ + a.scr_kc);
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
+    wc.sBucket = sBucket[warp];
+#ifdef MBE_PROFILE
+    for (int q = 0; q < kProfSlots; q++) wc.prof[q] = 0;
+    wc.last_busy = globaltimer_ns();
+#endif
     const bool donate = a.variant != MBE_NOWS;
+    const bool prefilter = a.variant != MBE_NOES;
     ResultAcc acc{};
-    uint32_t evals = 0;
+    uint32_t evals = 0, evals_reported = 0;
     Task t{};
     uint32_t my_path = 0;
-    while (pop_task(a, t, my_path)) {
+    for (;;) {
+        {
+            PROF_T0();
+            bool got = pop_task(a, t, my_path);
+            PROF_ADD(wc.prof, kProfPop);
+            if (!got) break;
+        }
+        PROF_T0();
         const uint32_t graph = ((const NodeHdr*)t.node)->graph;
         const GraphView G = a.graphs[graph];
         wc.arena_top = 0;
@@ -942,7 +1367,9 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
                 f0.next = t.plen ? p0 + 1 : t.begin;
                 f0.end = t.plen ? p0 + 1 : t.end;
                 f0.arena_mark = 0;
-                f0.pad = 0;
+                f0.cur = p0;
+                f0.mbase = 0;
+                f0.pmask = 0;
                 frames[0] = f0;
             }
         }
@@ -953,7 +1380,7 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
             uint32_t idx = __shfl_sync(kFull, my_path, j);
             uint32_t nxt = __shfl_sync(kFull, my_path, (j + 1) & 31);
             uint32_t mark = wc.arena_top;
-            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, wc, acc, true);
+            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, wc, acc, true, false);
             if (!co.rec) {
                 if (lane == 0) set_error(a, kErrReplay, j);
                 replay_ok = false;
@@ -968,32 +1395,79 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
                 nf.next = last ? t.begin : nxt + 1;
                 nf.end = last ? t.end : nxt + 1;
                 nf.arena_mark = mark;
-                nf.pad = 0;
+                nf.cur = nxt;
+                nf.mbase = 0;
+                nf.pmask = 0;
                 frames[depth] = nf;
             }
             __syncwarp();
         }
         if (!replay_ok) depth = -1;
+        PROF_ADD(wc.prof, kProfReplay);
         while (depth >= 0) {
             Frame f = frames[depth];
-            if (f.next >= f.end) {
-                wc.arena_top = f.arena_mark;
-                depth--;
-                continue;
+            uint32_t child;
+            bool known_max = false;
+            if (f.pmask) {
+                // a child the batch prefilter found maximal
+                child = f.mbase + __ffs(f.pmask) - 1;
+                known_max = true;
+                if (lane == 0) {
+                    frames[depth].pmask = f.pmask & (f.pmask - 1);
+                    frames[depth].cur = child;
+                }
+                __syncwarp();
+            } else {
+                if (f.next >= f.end) {
+                    wc.arena_top = f.arena_mark;
+                    depth--;
+                    continue;
+                }
+                if (donate && (evals & 3u) == 0) {
+                    // waiting warps = tickets taken beyond the tasks pushed
+                    uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
+                    if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) {
+                        PROF_T0();
+                        try_donate(a, frames, depth, wc);
+                        PROF_ADD(wc.prof, kProfDonate);
+                    }
+                    f = frames[depth];
+                    if (f.next >= f.end) continue;
+                }
+                const uint32_t* nd = (const uint32_t*)f.node;
+                if (prefilter && ((const NodeHdr*)nd)->W == 1) {
+                    PROF_T0();
+                    const RecView R = rec_view(nd);
+                    uint32_t nb = min(32u, f.end - f.next);
+                    uint32_t mask = prefilter_w1(R, f.next, nb, acc);
+                    PROF_ADD(wc.prof, kProfPrefilter);
+                    evals += nb;
+                    if (lane == 0) {
+                        frames[depth].next = f.next + nb;
+                        frames[depth].mbase = f.next;
+                        frames[depth].pmask = mask;
+                    }
+                    __syncwarp();
+                    if (evals - evals_reported >= 1024) {
+                        evals_reported = evals;
+                        if (lane == 0) atomicAdd(a.progress, 1ull);
+                    }
+                    continue;
+                }
+                child = f.next;
+                if (lane == 0) {
+                    frames[depth].next = f.next + 1;
+                    frames[depth].cur = child;
+                }
+                __syncwarp();
             }
-            if (donate && (evals & 3u) == 0) {
-                // waiting warps = tickets taken beyond the tasks pushed
-                uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
-                if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) try_donate(a, frames, depth, wc);
-                f = frames[depth];
-                if (f.next >= f.end) continue;
-            }
-            if (lane == 0) frames[depth].next = f.next + 1;
-            __syncwarp();
             uint32_t mark = wc.arena_top;
-            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, f.next, wc, acc, false);
+            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, wc, acc, false, known_max);
             evals++;
-            if ((evals & 1023u) == 0 && lane == 0) atomicAdd(a.progress, 1ull);
+            if (evals - evals_reported >= 1024) {
+                evals_reported = evals;
+                if (lane == 0) atomicAdd(a.progress, 1ull);
+            }
             if (co.rec) {
                 if (depth + 1 >= (int)a.max_frames) {
                     if (lane == 0) set_error(a, kErrFrames, depth);
@@ -1007,7 +1481,9 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
                     nf.next = 0;
                     nf.end = co.nchild;
                     nf.arena_mark = mark;
-                    nf.pad = 0;
+                    nf.cur = 0;
+                    nf.mbase = 0;
+                    nf.pmask = 0;
                     frames[depth] = nf;
                 }
                 __syncwarp();
@@ -1021,7 +1497,16 @@ __global__ void __launch_bounds__(kThreadsB) dfs_kernel(EngineArgs a) {
             atomicAdd(a.progress, 1ull);
         }
         __syncwarp();
+#ifdef MBE_PROFILE
+        wc.last_busy = globaltimer_ns();
+#endif
     }
+#ifdef MBE_PROFILE
+    if (lane == 0 && a.prof) {
+        for (int q = 0; q < kProfSlots; q++) atomicAdd(&a.prof[q], (unsigned long long)wc.prof[q]);
+        a.prof[kProfSlots + gw] = wc.last_busy;
+    }
+#endif
 }
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -1108,7 +1593,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     const uint32_t task_cap = (uint32_t)std::min<size_t>(roots.size() + q_margin + (size_t)cfg.extra_tasks, 0x7FFFFFFF);
     const uint32_t max_frames = cfg.max_frames;
     // Per-warp DFS arenas default to 4 MiB each (at most 30% of free device
-    // memory in total); the shared node pool starts at 2 GiB and is doubled
+    // memory in total); the shared node pool starts at 8 GiB and is doubled
     // (up to 60% of free memory) whenever a run exhausts it.
     size_t free_b = 0, tot_b = 0;
     MBE_CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
@@ -1118,7 +1603,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         if (const char* env = std::getenv("MBE_ARENA_WORDS")) want = std::strtoull(env, nullptr, 10);
         eb.arena_words = (uint32_t)std::max<uint64_t>(std::min(want, cap), 1u << 14) & ~31u;
     }
-    if (!eb.pool_words) eb.pool_words = 1ull << 29;
+    if (!eb.pool_words) eb.pool_words = 1ull << 31;
     const uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
     const uint32_t retry_cap = 1u << 16;
 
@@ -1182,6 +1667,17 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.error = &ctrl->error;
     a.error_info = &ctrl->error_info;
     a.timeout_ns = cfg.timeout_ns;
+#ifdef MBE_PROFILE
+    static unsigned long long* prof_dev = nullptr;
+    static size_t prof_n = 0;
+    if (prof_n < kProfSlots + nwarpsB) {
+        if (prof_dev) cudaFree(prof_dev);
+        prof_n = kProfSlots + nwarpsB;
+        MBE_CUDA_TRY(cudaMalloc(&prof_dev, sizeof(unsigned long long) * prof_n));
+    }
+    MBE_CUDA_TRY(cudaMemsetAsync(prof_dev, 0, sizeof(unsigned long long) * prof_n, s));
+    a.prof = prof_dev;
+#endif
 
     cudaEvent_t e0, e1, e2;
     MBE_CUDA_TRY(cudaEventCreate(&e0));
@@ -1245,7 +1741,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
                 while (kc < scr_n) kc <<= 1;
-                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc, 32);
+                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 5 * kc, 32);
                 if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
                 a.scratch = (uint32_t*)eb.scratch.ptr;
                 a.scratch_words = (uint32_t)sw;
@@ -1321,6 +1817,26 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     if (result != MBE_OK) return result;
     MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
     io->d2h += sizeof(ResultAcc) * ng;
+#ifdef MBE_PROFILE
+    {
+        unsigned long long hp[kProfSlots];
+        MBE_CUDA_TRY(cudaMemcpy(hp, a.prof, sizeof hp, cudaMemcpyDeviceToHost));
+        static const char* names[] = {"pop", "replay", "donate", "prefilter", "qscan", "expand", "build"};
+        unsigned long long tot = 0;
+        for (int q = 0; q < kProfSections; q++) tot += hp[2 * q];
+        for (int q = 0; q < kProfSections; q++)
+            std::fprintf(stderr, "prof %-10s cycles %14llu (%5.1f%%) events %12llu\n", names[q], hp[2 * q],
+                         tot ? 100.0 * hp[2 * q] / tot : 0.0, hp[2 * q + 1]);
+        std::vector<unsigned long long> ex(nwarpsB);
+        MBE_CUDA_TRY(cudaMemcpy(ex.data(), a.prof + kProfSlots, sizeof(unsigned long long) * nwarpsB,
+                                cudaMemcpyDeviceToHost));
+        std::sort(ex.begin(), ex.end());
+        unsigned long long t0 = ex.front();
+        std::fprintf(stderr, "prof warps last busy after the first (ms): p10 %.3f p50 %.3f p90 %.3f p99 %.3f max %.3f\n",
+                     (ex[nwarpsB / 10] - t0) / 1e6, (ex[nwarpsB / 2] - t0) / 1e6, (ex[nwarpsB * 9 / 10] - t0) / 1e6,
+                     (ex[nwarpsB * 99 / 100] - t0) / 1e6, (ex.back() - t0) / 1e6);
+    }
+#endif
     if (stats) {
         stats->ms_expand = ms_a;
         stats->ms_dfs = ms_b;

@@ -32,7 +32,7 @@ __host__ __device__ inline uint32_t pad4(uint32_t x) { return (x + 3u) & ~3u; }
 
 // record layout (32-bit words):
 //   [0,16)      header
-//   wmap[W]     root word index of each word
+//   wmap[W]     root word index of each word (lmap[32] when packed)
 //   Lm[W]       L as bits per word
 //   cand[n]     candidate ranks; [0,nq) = Q part, [nq,n) = P part
 //   cnt[n]      |N(v) n L| (P part)
@@ -49,12 +49,32 @@ struct NodeHdr {
     unsigned long long sR;
     uint32_t words;
     uint32_t rlist;   // word offset (from record start) of the R list, 0 if absent
-    uint32_t pad[4];
+    uint32_t flags;   // kRecPacked: W == 1 and bit t of L is root bit lmap[t]
+    uint32_t pad[3];
 };
 static_assert(sizeof(NodeHdr) == kHdrWords * 4, "header size");
 
-__host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n) {
-    return kHdrWords + 2ull * pad4(W) + 2ull * pad4(n) + (((uint64_t)W * n + 3) & ~3ull);
+constexpr uint32_t kRecPacked = 1;
+
+// Section buckets of the optional cycle profile (-DMBE_PROFILE): cycles
+// spent and events counted per section, summed over warps.
+enum : int {
+    kProfPop = 0,        // waiting for / taking a task
+    kProfReplay,         // re-deriving donated paths
+    kProfDonate,         // donating
+    kProfPrefilter,      // batch maximality prefilter (one-word rows)
+    kProfQscan,          // L_i + maximality scan of single evaluations
+    kProfExpand,         // expansion (P scan) + hash of maximal children
+    kProfBuild,          // child record construction
+    kProfSections,
+    kProfSlots = 2 * kProfSections
+};
+
+// A packed record (|L| <= 32) keeps its L bits dense in one word and maps
+// bit t to root bit lmap[t] (32 words); otherwise word k of a row is root
+// word wmap[k].
+__host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n, bool packed = false) {
+    return kHdrWords + (packed ? 32ull : pad4(W)) + pad4(W) + 2ull * pad4(n) + (((uint64_t)W * n + 3) & ~3ull);
 }
 
 // A unit of work: children [begin, end) of the node reached from the pool
@@ -71,10 +91,12 @@ static_assert(sizeof(Task) == 128, "task size");
 
 struct Frame {
     unsigned long long node;
-    uint32_t next, end;
+    uint32_t next, end;       // children [next, end) not yet looked at
     uint32_t arena_mark;      // arena top to restore when the frame pops
-    uint32_t pad;
+    uint32_t cur;             // child the next frame expands (donation paths)
+    uint32_t mbase, pmask;    // children mbase + bit of pmask: known maximal, pending
 };
+static_assert(sizeof(Frame) == 32, "frame size");
 
 struct ResultAcc {
     unsigned long long count, hash, nodes, words, words_expand;
@@ -136,6 +158,8 @@ struct EngineArgs {
     uint32_t scr_n;            // candidate bound the scratch is laid out for
     uint32_t scr_kc;           // key-array capacity (power of two >= scr_n)
     uint32_t max_W;            // largest universe word count
+    // section cycle counters (builds with -DMBE_PROFILE only; else null)
+    unsigned long long* prof;  // [kProfSlots]
     // results
     ResultAcc* results;        // [n_graphs]
     int* error;

@@ -59,3 +59,22 @@ def test_gpu_matches_fixture(engine, name):
         r = engine.enumerate(g, variant)
         assert r.count == EXPECTED[name]["count"], variant
         assert f"{r.hash:#018x}" == EXPECTED[name]["hash"], variant
+
+
+GENERATED = json.load(open(os.path.join(GOLD, "reference_generated.json")))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(GENERATED))
+def test_gpu_matches_reference_on_generated_graphs(engine, name):
+    """Counts the reference's own kernels printed on the synthetic workloads
+    (tests/golden/reference_generated.json); all four variants must agree
+    on count and hash."""
+    rec = GENERATED[name]
+    g = cm.Graph.generate(**rec["generator"])
+    results = {v: engine.enumerate(g, v) for v in ["cuMBE", "noRS", "noES", "noWS"]}
+    for v, r in results.items():
+        assert r.count % 2**32 == rec["reference"]["cuMBE"]["count"] % 2**32, v
+        assert r.hash == results["cuMBE"].hash, v
+    if "oracle" in rec:
+        assert f"{results['cuMBE'].hash:#018x}" == rec["oracle"]["hash"]
