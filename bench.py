@@ -140,6 +140,84 @@ def cpu_baseline(g, wl, threads, stride_mult=1):
     return r, dt, stride
 
 
+def batched_leg(eng, n_graphs=4096):
+    """Batched workload: n_graphs graphs (workloads.batch) in one launch pair
+    vs one launch pair per graph; per-graph counts and hashes must agree."""
+    import cumbe_gb300 as cm
+    from cumbe_gb300 import workloads
+    ps = workloads.batch(n_graphs)
+    gs = [cm.Graph.generate(**p) for p in ps]
+    for g in gs:
+        eng.upload(g)
+    res, ms = eng.batch(gs)
+    plain_ms = 0.0
+    mismatches = 0
+    for g, r in zip(gs, res):
+        q = eng.enumerate(g)
+        plain_ms += q.ms
+        mismatches += (q.count, q.hash) != (r.count, r.hash)
+    total = sum(r.count for r in res)
+    for g in gs:
+        eng.release(g)
+    return {"graphs": n_graphs, "bicliques": total, "batched_ms": ms, "plain_ms": plain_ms,
+            "batched_bicliques_per_s": total / (ms / 1e3), "plain_bicliques_per_s": total / (plain_ms / 1e3),
+            "per_graph_mismatches": mismatches,
+            "workload": "4,096 uniform random graphs, |U| log-uniform [50,5000], |V|=|U|/2, "
+                        "density log-uniform [0.002,0.05], seeds 0..4095"}
+
+
+def served_leg(rate=2000.0, n_requests=4000, seed=11):
+    """Poisson request stream against a device-resident pool: continuous
+    batching (2 slots on half the GPU each, up to 256 requests per launch)
+    vs one request per launch on the whole GPU.  Half the requests are
+    thresholded (|A| >= a, |B| >= b, a, b uniform in 1..5)."""
+    import numpy as np
+    import cumbe_gb300 as cm
+    from cumbe_gb300 import workloads
+    pool = [cm.Graph.generate(**workloads.SINGLE["power_law_2k_1k"])]
+    pool += [cm.Graph.generate(**p) for p in workloads.batch(4096) if p["n_rows"] <= 1000]
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    picks = rng.integers(0, len(pool), n_requests)
+    thr = [(0, 0) if rng.random() < 0.5 else (int(rng.integers(1, 6)), int(rng.integers(1, 6)))
+           for _ in range(n_requests)]
+
+    def run(slots, max_batch, bpsm):
+        srv = cm.Server(0, slots=slots, max_batch=max_batch, blocks_per_sm=bpsm)
+        try:
+            gids = [srv.add_graph(g) for g in pool]
+            t0 = time.perf_counter()
+            due = 0.0
+            for i in range(n_requests):
+                due += gaps[i]
+                while time.perf_counter() - t0 < due:
+                    pass
+                a, b = thr[i]
+                srv.submit(gids[picks[i]], a, b)
+            out = []
+            while len(out) < n_requests:
+                out += srv.poll()
+                time.sleep(0.001)
+        finally:
+            srv.stop()
+        lat = np.array([r["done_s"] - r["submit_s"] for r in out]) * 1e3
+        span = max(r["done_s"] for r in out) - min(r["submit_s"] for r in out)
+        tot = sum(r["count"] for r in out)
+        ok = all(r["status"] == 0 for r in out)
+        res = {(r["request"]): (r["count"], r["hash"]) for r in out}
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "requests_per_s": n_requests / span, "bicliques_per_s": tot / span, "all_ok": ok,
+                "mean_batch": float(np.mean([r["batch_size"] for r in out]))}, res
+
+    cont, r1 = run(2, 256, 1)
+    plain, r2 = run(1, 1, 0)
+    same = [r1[k] for k in sorted(r1)] == [r2[k] for k in sorted(r2)]
+    return {"rate_req_per_s": rate, "requests": n_requests, "pool_graphs": len(pool),
+            "continuous_batching": cont, "one_request_per_launch": plain,
+            "results_identical": same,
+            "pool": "the 2,000 x 1,000 power-law graph + the batch graphs with |U| <= 1000"}
+
+
 def run_reference(args, wl, rank, world):
     """--impl reference: the CPU restatement of the reference's search."""
     if rank != 0:
@@ -180,6 +258,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--variant", default="cuMBE", choices=["cuMBE", "noRS", "noES", "noWS"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -274,6 +354,10 @@ def main():
             "e2e": e2e, "roofline": roofline,
             "gpu_launches": c1["launches"] - c0["launches"],
             "clocks": clocks}
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_leg(eng)
+    if rank == 0 and not args.no_served:
+        line["served"] = served_leg()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rc, dt, stride = cpu_baseline(g, wl, threads)

@@ -66,6 +66,18 @@ class _Result(ctypes.Structure):
                 ("ms", ctypes.c_float), ("ms_prep", ctypes.c_float)]
 
 
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("variant", ctypes.c_uint32), ("mem_budget", ctypes.c_uint64)]
+
+
+class _RequestResult(ctypes.Structure):
+    _fields_ = [("request", ctypes.c_uint64), ("graph", ctypes.c_uint32), ("status", ctypes.c_uint32),
+                ("count", ctypes.c_uint64), ("hash", ctypes.c_uint64), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("done_s", ctypes.c_double), ("batch_size", ctypes.c_uint32),
+                ("slot", ctypes.c_uint32)]
+
+
 # Every symbol include/mbe.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _U64P = ctypes.POINTER(ctypes.c_uint64)
@@ -91,6 +103,13 @@ SIGNATURES = {
     "mbe_variant_from_name": (ctypes.c_int, [ctypes.c_char_p]),
     "mbe_ctx_last_grid": (ctypes.c_int, [_VP, _U32P, _U32P, _U32P]),
     "mbe_ctx_counters": (ctypes.c_int, [_VP, _U64P, _U64P, _U64P]),
+    "mbe_server_start": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_ServerConfig), ctypes.POINTER(_VP)]),
+    "mbe_server_add_graph": (ctypes.c_int, [_VP, _VP, _U32P]),
+    "mbe_server_estimate": (ctypes.c_int, [_VP, ctypes.c_uint32, _U64P]),
+    "mbe_server_submit": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _U64P]),
+    "mbe_server_poll": (ctypes.c_int, [_VP, ctypes.POINTER(_RequestResult), ctypes.c_uint32, _U32P]),
+    "mbe_server_clock": (ctypes.c_double, [_VP]),
+    "mbe_server_stop": (ctypes.c_int, [_VP]),
     "mbe_enumerate_static": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, _VP, _VP, _VP, _VP, ctypes.c_int,
                                             _VP, _VP]),
 }
@@ -276,3 +295,50 @@ def biclique_hash(rows, cols) -> int:
     r1 = r if r.size else np.zeros(1, np.uint32)
     c1 = c if c.size else np.zeros(1, np.uint32)
     return int(lib().mbe_biclique_hash(r1.ctypes.data_as(_U32P), r.size, c1.ctypes.data_as(_U32P), c.size))
+
+
+class Server:
+    """Continuous-batching enumeration service over device-resident graphs
+    (mbe_server_*).  Requests are answered asynchronously; poll() returns
+    finished ones with their timestamps on the server clock."""
+
+    def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 1,
+                 variant: str = "cuMBE", mem_budget: int = 0):
+        cfg = _ServerConfig(slots, max_batch, blocks_per_sm, VARIANTS[variant], mem_budget)
+        self._h = _VP()
+        _check(lib().mbe_server_start(device, ctypes.byref(cfg), ctypes.byref(self._h)), "mbe_server_start")
+
+    def add_graph(self, g: Graph) -> int:
+        gid = ctypes.c_uint32()
+        _check(lib().mbe_server_add_graph(self._h, g.handle, ctypes.byref(gid)), "mbe_server_add_graph")
+        return gid.value
+
+    def estimate(self, gid: int) -> int:
+        b = ctypes.c_uint64()
+        _check(lib().mbe_server_estimate(self._h, gid, ctypes.byref(b)), "mbe_server_estimate")
+        return b.value
+
+    def submit(self, gid: int, min_rows: int = 0, min_cols: int = 0) -> int:
+        rid = ctypes.c_uint64()
+        _check(lib().mbe_server_submit(self._h, gid, min_rows, min_cols, ctypes.byref(rid)), "mbe_server_submit")
+        return rid.value
+
+    def poll(self, cap: int = 4096) -> list[dict]:
+        buf = (_RequestResult * cap)()
+        n = ctypes.c_uint32()
+        _check(lib().mbe_server_poll(self._h, buf, cap, ctypes.byref(n)), "mbe_server_poll")
+        return [{f: getattr(buf[i], f) for f, _ in _RequestResult._fields_} for i in range(n.value)]
+
+    def clock(self) -> float:
+        return lib().mbe_server_clock(self._h)
+
+    def stop(self):
+        if self._h and self._h.value:
+            _check(lib().mbe_server_stop(self._h), "mbe_server_stop")
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass

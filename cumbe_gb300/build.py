@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libmbe.so")
 CLI = os.path.join(HERE, "mbe")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["graph_host.cpp", "graph_dev.cu", "engine.cu", "capi.cu", "capi_static.cu"]
+SOURCES = ["graph_host.cpp", "graph_dev.cu", "engine.cu", "capi.cu", "capi_static.cu", "server.cu"]
 
 
 def nvcc() -> str:

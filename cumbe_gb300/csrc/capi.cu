@@ -124,20 +124,18 @@ extern "C" mbe_status mbe_graph_release(mbe_ctx* ctx, const mbe_graph* g) {
     return MBE_OK;
 }
 
-static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
-                             const mbe_opts* opts, mbe_result* out, float* total_ms) {
-    if (opts && (opts->flags & MBE_OPT_EMIT))
-        return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT is not supported by this build");
-    mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
-    if (st) return st;
-    std::vector<const DeviceGraph*> devs(n);
+namespace mbe {
+
+// Enumerates the maximal bicliques of the resident graphs `devs` (one
+// result per entry; an entry may repeat a graph).  Roots of all graphs are
+// expanded heaviest first in one launch pair.  Thresholds are stated in
+// file orientation, so a list mixing orientations with thresholds runs
+// once per orientation group.
+mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
+                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats) {
+    const uint32_t n = (uint32_t)devs.size();
     bool any_swapped = false, any_plain = false;
-    for (uint32_t i = 0; i < n; i++) {
-        if (!graphs[i]) return fail(MBE_ERR_INVALID_ARG, "null graph");
-        if ((st = ensure_resident(ctx, graphs[i], &devs[i]))) return st;
-        (devs[i]->swapped ? any_swapped : any_plain) = true;
-    }
-    // Roots, heaviest first (rank order is degree order within a graph).
+    for (const DeviceGraph* d : devs) (d->swapped ? any_swapped : any_plain) = true;
     std::vector<uint2> roots;
     size_t total = 0;
     for (uint32_t i = 0; i < n; i++) total += devs[i]->nR - devs[i]->n_isolated;
@@ -148,25 +146,21 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         std::stable_sort(roots.begin(), roots.end(), [&](const uint2& a, const uint2& b) {
             return devs[a.x]->deg_by_rank[a.y] > devs[b.x]->deg_by_rank[b.y];
         });
-    // Thresholds are stated in file orientation; a batch mixing orientations
-    // is enumerated per orientation group.
-    std::vector<ResultAcc> acc(n, ResultAcc{});
-    float ms = 0;
-    EngineStats stats;
-    bool thresholds = opts && (opts->min_rows || opts->min_cols);
+    acc.assign(n, ResultAcc{});
+    stats = EngineStats{};
+    const bool thresholds = opts && (opts->min_rows || opts->min_cols);
+    const bool split = thresholds && any_swapped && any_plain;
     for (int pass = 0; pass < 2; pass++) {
         bool sw = pass == 1;
         if (sw ? !any_swapped : !any_plain) continue;
         std::vector<uint2> sel;
-        if (thresholds && any_swapped && any_plain) {
+        if (split)
             for (const uint2& r : roots)
                 if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
-        }
-        const std::vector<uint2>& use = (thresholds && any_swapped && any_plain) ? sel : roots;
         EngineConfig cfg = make_config(variant, opts, sw);
         std::vector<ResultAcc> part;
         EngineStats ps;
-        st = engine_run(ctx->eb, ctx->stream, cfg, devs, use, part, &ps, &ctx->io);
+        mbe_status st = engine_run(eb, s, cfg, devs, split ? sel : roots, part, &ps, io);
         if (st != MBE_OK) return st;
         for (uint32_t i = 0; i < n; i++) {
             acc[i].count += part[i].count;
@@ -175,14 +169,32 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
             acc[i].words += part[i].words;
             acc[i].words_expand += part[i].words_expand;
         }
-        ms += ps.ms_expand + ps.ms_dfs;
         stats.ms_expand += ps.ms_expand;
         stats.ms_dfs += ps.ms_dfs;
         stats.chunks += ps.chunks;
         stats.grid_a = ps.grid_a;
         stats.grid_b = ps.grid_b;
-        if (!(thresholds && any_swapped && any_plain)) break;
+        if (!split) break;
     }
+    return MBE_OK;
+}
+
+}  // namespace mbe
+
+static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
+                             const mbe_opts* opts, mbe_result* out, float* total_ms) {
+    if (opts && (opts->flags & MBE_OPT_EMIT))
+        return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT is not supported by this build");
+    mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (st) return st;
+    std::vector<const DeviceGraph*> devs(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (!graphs[i]) return fail(MBE_ERR_INVALID_ARG, "null graph");
+        if ((st = ensure_resident(ctx, graphs[i], &devs[i]))) return st;
+    }
+    std::vector<ResultAcc> acc;
+    EngineStats stats;
+    if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, devs, variant, opts, acc, stats))) return st;
     ctx->last_stats = stats;
     for (uint32_t i = 0; i < n; i++) {
         mbe_result& r = out[i];
@@ -195,7 +207,7 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         r.ms = stats.ms_expand + stats.ms_dfs;
         r.ms_prep = stats.ms_expand;
     }
-    if (total_ms) *total_ms = ms;
+    if (total_ms) *total_ms = stats.ms_expand + stats.ms_dfs;
     return MBE_OK;
 }
 

@@ -50,6 +50,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                       const std::vector<const DeviceGraph*>& graphs, const std::vector<uint2>& roots,
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io);
 
+// Enumeration of resident graphs with opts applied (capi.cu).
+mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
+                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats);
+
 // Raw launchers of the two enumeration kernels (256 threads per block;
 // dfs_kernel runs 8 warps per block).
 cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s);

@@ -210,6 +210,53 @@ MBE_API const char* mbe_variant_name(mbe_variant v);
  * MBE_CUMBE as src/main.cu:122 does. */
 MBE_API mbe_variant mbe_variant_from_name(const char* name);
 
+/* ---- serving: continuous batching of enumeration requests -------------- */
+
+/* No reference counterpart (the reference runs one graph per process).
+ * Graphs are added once and stay resident; requests name a graph and
+ * optional thresholds and are answered asynchronously.  `slots` worker
+ * threads each own a stream and engine buffers and run on a share of the
+ * GPU (`blocks_per_sm` DFS blocks per SM), so batches of different slots
+ * overlap on the device.  A free slot takes the oldest waiting request
+ * plus every later waiting request with the same thresholds, up to
+ * `max_batch`, while the estimated search memory of admitted requests stays
+ * within `mem_budget` bytes (a request larger than the budget runs alone). */
+typedef struct mbe_server mbe_server;
+
+typedef struct mbe_server_config {
+    uint32_t slots;              /* default 2                               */
+    uint32_t max_batch;          /* default 256 (1 = one request per launch) */
+    uint32_t blocks_per_sm;      /* default 1; 0 = the whole GPU per slot   */
+    uint32_t variant;            /* mbe_variant                             */
+    uint64_t mem_budget;         /* default 120 GB                          */
+} mbe_server_config;
+
+typedef struct mbe_request_result {
+    uint64_t request;
+    uint32_t graph;
+    uint32_t status;             /* mbe_status of the request               */
+    uint64_t count;
+    uint64_t hash;
+    double submit_s, start_s, done_s;  /* server clock, seconds            */
+    uint32_t batch_size;         /* requests in the launch that served it   */
+    uint32_t slot;
+} mbe_request_result;
+
+MBE_API mbe_status mbe_server_start(int device, const mbe_server_config* cfg, mbe_server** out);
+/* Uploads g (device-resident for the server's lifetime); *graph_id names it. */
+MBE_API mbe_status mbe_server_add_graph(mbe_server* s, const mbe_graph* g, uint32_t* graph_id);
+/* Estimated bytes of search memory of a request on graph_id. */
+MBE_API mbe_status mbe_server_estimate(mbe_server* s, uint32_t graph_id, uint64_t* bytes);
+/* Queues a request (thresholds |A| >= min_rows, |B| >= min_cols); never blocks. */
+MBE_API mbe_status mbe_server_submit(mbe_server* s, uint32_t graph_id, uint32_t min_rows, uint32_t min_cols,
+                                     uint64_t* request_id);
+/* Moves up to cap finished requests into out, oldest first. */
+MBE_API mbe_status mbe_server_poll(mbe_server* s, mbe_request_result* out, uint32_t cap, uint32_t* n_out);
+/* Seconds since the server started (the clock of mbe_request_result). */
+MBE_API double mbe_server_clock(mbe_server* s);
+/* Finishes every queued request, stops the workers and frees the server. */
+MBE_API mbe_status mbe_server_stop(mbe_server* s);
+
 /* ---- allocation-free enumeration --------------------------------------- */
 
 /* Working memory of mbe_enumerate_static: one array compiled into the

@@ -1,0 +1,54 @@
+"""Serving (mbe_server_*): continuous batching over device-resident graphs.
+Each request's count and hash are the same alone and in the mix."""
+import time
+
+import numpy as np
+import pytest
+
+import cumbe_gb300 as cm
+from cumbe_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _drain(srv, n, timeout=120.0):
+    out = []
+    t0 = time.time()
+    while len(out) < n:
+        out += srv.poll()
+        if time.time() - t0 > timeout:
+            raise TimeoutError(f"{len(out)}/{n} requests finished")
+        time.sleep(0.002)
+    return out
+
+
+@pytest.mark.parametrize("slots,max_batch", [(2, 256), (1, 1), (3, 8)])
+def test_results_same_alone_and_in_the_mix(engine, slots, max_batch):
+    rng = np.random.default_rng(17)
+    graphs = [cm.Graph.generate(**workloads.batch_params(s)) for s in range(24)
+              if workloads.batch_params(s)["n_rows"] <= 1500]
+    graphs.append(cm.Graph.generate(**workloads.SINGLE["power_law_2k_1k"]))
+    srv = cm.Server(0, slots=slots, max_batch=max_batch)
+    try:
+        gids = [srv.add_graph(g) for g in graphs]
+        reqs = []
+        for _ in range(150):
+            k = int(rng.integers(len(gids)))
+            a, b = (0, 0) if rng.random() < 0.5 else (int(rng.integers(1, 6)), int(rng.integers(1, 6)))
+            reqs.append((srv.submit(gids[k], a, b), k, a, b))
+            if rng.random() < 0.3:
+                time.sleep(0.0005)
+        res = {r["request"]: r for r in _drain(srv, len(reqs))}
+    finally:
+        srv.stop()
+    alone = {}
+    for rid, k, a, b in reqs:
+        if (k, a, b) not in alone:
+            r = engine.enumerate(graphs[k], min_rows=a, min_cols=b)
+            alone[(k, a, b)] = (r.count, r.hash)
+        got = res[rid]
+        assert got["status"] == 0
+        assert (got["count"], got["hash"]) == alone[(k, a, b)], (k, a, b)
+        assert got["done_s"] >= got["start_s"] >= got["submit_s"]
+    if max_batch > 1:
+        assert max(r["batch_size"] for r in res.values()) > 1  # requests were batched
