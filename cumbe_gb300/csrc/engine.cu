@@ -37,6 +37,9 @@ constexpr int kThreadsB = kWarpsB * 32;
 constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
 constexpr uint32_t kKeepWindow = 32;     // Q rows a dropped Q row is tested against
+constexpr uint32_t kDonateSlabMax = 8192;      // arena records up to this size are copied into a slab
+constexpr uint32_t kDonateCopyMax = 1u << 20;  // larger ones up to this size by a direct pool allocation
+constexpr uint32_t kSlabWords = 1u << 16;      // pool slab a warp takes for donation copies
 
 __device__ __forceinline__ void set_error(const EngineArgs& a, int code, unsigned long long info) {
     if (atomicCAS(a.error, 0, code) == 0) *a.error_info = info;
@@ -80,11 +83,20 @@ __device__ bool push_task(const EngineArgs& a, Task t) {
 }
 
 #ifdef MBE_PROFILE
+#define PROF_TAB(cls, c0, v)                                                                              \
+    do {                                                                                                  \
+        if (lane == 0) {                                                                                  \
+            unsigned tb__ = (unsigned)min((globaltimer_ns() - wc.t_start) / kProfTabNs, (unsigned long long)kProfTB - 1); \
+            atomicAdd(&sTab[(tb__ * kProfTC + (cls)) * 2], (unsigned long long)(v));                      \
+            atomicAdd(&sTab[(tb__ * kProfTC + (cls)) * 2 + 1], 1ull);                                     \
+        }                                                                                                 \
+    } while (0)
 #define PROF_T0() long long prof_t0__ = clock64()
 #define PROF_ADD(acc_arr, sec) do { (acc_arr)[2 * (sec)] += clock64() - prof_t0__; (acc_arr)[2 * (sec) + 1]++; prof_t0__ = clock64(); } while (0)
 #else
 #define PROF_T0() do {} while (0)
 #define PROF_ADD(acc_arr, sec) do {} while (0)
+#define PROF_TAB(cls, c0, v) do {} while (0)
 #endif
 
 // Bump allocation from the node pool; ~0 when it does not fit.  Sizes are
@@ -551,9 +563,11 @@ struct WarpCtx {
     uint32_t* sNz;
     uint32_t* scrPack;     // 5 x kc words: qrow, qpos, srow, spos, porder
     uint32_t* sBucket;     // 32 words of shared memory
+    unsigned long long slab_off, slab_end;  // this warp's slab of the node pool (donation copies)
 #ifdef MBE_PROFILE
     long long prof[kProfSlots];
     unsigned long long last_busy;  // globaltimer when the warp last finished a task
+    unsigned long long t_start;    // globaltimer at kernel start
 #endif
 };
 
@@ -780,23 +794,23 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     ChildOut out{nullptr, 0, 0};
     // Q' = rows of Q u P[0..i) meeting L_i, packed, in parent order
     uint32_t m = 0;
-    for (uint32_t base = 0; base < xi; base += 64) {  // two chunks per step: independent loads
-        uint32_t c0 = base + lane, c1 = base + 32 + lane;
-        uint32_t r0 = c0 < xi ? packed_row(M, n, Nz, Li, nnz, c0, plan0) : 0u;
-        uint32_t r1 = c1 < xi ? packed_row(M, n, Nz, Li, nnz, c1, plan0) : 0u;
-        unsigned b0 = __ballot_sync(kFull, r0 != 0), b1 = __ballot_sync(kFull, r1 != 0);
-        if (r0) {
-            uint32_t p = m + __popc(b0 & lanemask_lt());
-            qrow[p] = r0;
-            qpos[p] = c0;
+    for (uint32_t base = 0; base < xi; base += 128) {  // four chunks per step: independent loads
+        uint32_t r[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            uint32_t c = base + 32 * q + lane;
+            r[q] = c < xi ? packed_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
         }
-        m += __popc(b0);
-        if (r1) {
-            uint32_t p = m + __popc(b1 & lanemask_lt());
-            qrow[p] = r1;
-            qpos[p] = c1;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            unsigned b = __ballot_sync(kFull, r[q] != 0);
+            if (r[q]) {
+                uint32_t p = m + __popc(b & lanemask_lt());
+                qrow[p] = r[q];
+                qpos[p] = base + 32 * q + lane;
+            }
+            m += __popc(b);
         }
-        m += __popc(b1);
     }
     __syncwarp();
     acc.words += (unsigned long long)xi * nnz;
@@ -1261,12 +1275,17 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, R
     return __ballot_sync(kFull, active && !covered);
 }
 
-// Gives the upper half of the remaining children of the shallowest frame
-// with at least donate_min of them to a waiting warp.  A frame whose record
-// is in the node pool is shared by pointer; a frame whose record lives in
-// this warp's arena is described by the child-index path from frame 0
-// (always a pool record), which the receiver replays.  Warp-collective.
-__device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc) {
+// Splits the remaining children of the shallowest frame with at least
+// donate_min of them among the donor and up to 31 waiting warps (one task
+// per lane, equal shares; the donor keeps the lowest indices).  A frame whose
+// record is in the node pool is shared by pointer.  A frame whose record lives
+// in this warp's arena is copied once into the pool when it fits (pool below
+// 60%: small records into this warp's slab, larger ones by a direct
+// allocation) and shared by pointer; otherwise it is described by the
+// child-index path from frame 0 (always a pool record), which each receiver
+// replays.  Warp-collective.
+__device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc,
+                                        uint32_t waiters) {
     unsigned lane = lane_id();
     int k = -1;
     for (int base = 0; base <= depth && k < 0; base += 32) {
@@ -1283,22 +1302,74 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
     }
     if (k < 0) return;
     Frame fr = frames[k];
-    uint32_t rem = fr.end - fr.next;
-    uint32_t give = rem / 2;
-    if (give == 0) return;
-    uint32_t mid = fr.end - give;
+    const uint32_t rem = fr.end - fr.next;
+    const uint32_t pieces = min(min(waiters, 31u), rem - 1);  // tasks given away
+    if (pieces == 0) return;
+    const uint32_t share = rem / (pieces + 1);
+    const uint32_t mid = fr.end - pieces * share;
     uint32_t* nd = (uint32_t*)fr.node;
     bool in_arena = nd >= wc.arena && nd < wc.arena + a.arena_words;
+    unsigned long long copy_off = ~0ull;
+    if (in_arena && a.donate_copy) {
+        const uint32_t words = ((const NodeHdr*)nd)->words;
+        const unsigned long long need = (words + 31ull) & ~31ull;  // whole 128-byte lines
+        const unsigned long long limit = a.pool_words / 10 * 6;
+        if (words <= kDonateSlabMax) {
+            if (wc.slab_off + need > wc.slab_end) {
+                unsigned long long base = ~0ull;
+                if (lane == 0 && ld_volatile(a.pool_top) + kSlabWords < limit)
+                    base = atomicAdd(a.pool_top, (unsigned long long)kSlabWords);
+                base = __shfl_sync(kFull, base, 0);
+                if (base != ~0ull && base + kSlabWords <= a.pool_words) {
+                    wc.slab_off = base;
+                    wc.slab_end = base + kSlabWords;
+                }
+            }
+            if (wc.slab_off + need <= wc.slab_end) {
+                copy_off = wc.slab_off;
+                wc.slab_off += need;
+            }
+        } else if (words <= kDonateCopyMax) {
+            unsigned long long base = ~0ull;
+            if (lane == 0 && ld_volatile(a.pool_top) + need < limit) base = atomicAdd(a.pool_top, need);
+            base = __shfl_sync(kFull, base, 0);
+            if (base != ~0ull && base + need <= a.pool_words) copy_off = base;
+        }
+        if (copy_off != ~0ull) {
+            const uint4* s4 = (const uint4*)nd;
+            uint4* d4 = (uint4*)(a.pool + copy_off);
+            const uint32_t n4 = words / 4;
+            uint32_t w = lane;
+            for (; w + 96 < n4; w += 128) {  // four independent lines in flight
+                uint4 v0 = s4[w], v1 = s4[w + 32], v2 = s4[w + 64], v3 = s4[w + 96];
+                d4[w] = v0;
+                d4[w + 32] = v1;
+                d4[w + 64] = v2;
+                d4[w + 96] = v3;
+            }
+            for (; w < n4; w += 32) d4[w] = s4[w];
+            __threadfence();
+            __syncwarp();
+        }
+    }
     // path element j = the child of frame j that frame j+1 expands (k <= kMaxPath <= 31)
     uint32_t pe = ((int)lane < k) ? frames[lane].cur : 0u;
     Task t{};
-    t.begin = mid;
-    t.end = fr.end;
-    t.node = in_arena ? frames[0].node : fr.node;
-    t.plen = in_arena ? (uint32_t)k : 0u;
+    if (!in_arena) {
+        t.node = fr.node;
+        t.plen = 0;
+    } else if (copy_off != ~0ull) {
+        t.node = (unsigned long long)(a.pool + copy_off);
+        t.plen = 0;
+    } else {
+        t.node = frames[0].node;
+        t.plen = (uint32_t)k;
+    }
     for (int j = 0; j < (int)t.plen; j++) t.path[j] = __shfl_sync(kFull, pe, j);
-    if (lane == 0) {
-        frames[k].end = mid;
+    if (lane == 0) frames[k].end = mid;
+    if (lane < pieces) {
+        t.begin = mid + lane * share;
+        t.end = t.begin + share;
         push_task(a, t);
     }
     __syncwarp();
@@ -1314,6 +1385,21 @@ __device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, Resu
     }
     acc = ResultAcc{};
 }
+
+#ifdef MBE_PROFILE
+// Spreads one idle interval [w0, w1) over the 4 ms bins of the kernel-time
+// histogram (idle ns per bin, then waits ending per bin).
+__device__ void prof_idle(const EngineArgs& a, unsigned long long t0, unsigned long long w0, unsigned long long w1) {
+    unsigned long long* hist = a.prof + kProfSlots + a.prof_warps;
+    unsigned long long s = w0 - t0, e = w1 - t0;
+    for (unsigned long long b = s / kProfBinNs; b < kProfBins && b * kProfBinNs < e; b++) {
+        unsigned long long lo = max(s, b * kProfBinNs), hi = min(e, (b + 1) * kProfBinNs);
+        atomicAdd(&hist[b], hi - lo);
+    }
+    unsigned long long be = e / kProfBinNs;
+    if (be < kProfBins) atomicAdd(&hist[kProfBins + be], 1ull);
+}
+#endif
 
 __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
     __shared__ uint32_t sLi[kWarpsB][kSmemW];
@@ -1337,9 +1423,14 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
     wc.sBucket = sBucket[warp];
+    wc.slab_off = wc.slab_end = 0;
 #ifdef MBE_PROFILE
+    __shared__ unsigned long long sTab[kProfTB * kProfTC * 2];
+    for (int i = threadIdx.x; i < kProfTB * kProfTC * 2; i += blockDim.x) sTab[i] = 0;
+    __syncthreads();
     for (int q = 0; q < kProfSlots; q++) wc.prof[q] = 0;
     wc.last_busy = globaltimer_ns();
+    wc.t_start = wc.last_busy;
 #endif
     const bool donate = a.variant != MBE_NOWS;
     const bool prefilter = a.variant != MBE_NOES;
@@ -1350,8 +1441,14 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
     for (;;) {
         {
             PROF_T0();
+#ifdef MBE_PROFILE
+            unsigned long long w0 = globaltimer_ns();
+#endif
             bool got = pop_task(a, t, my_path);
             PROF_ADD(wc.prof, kProfPop);
+#ifdef MBE_PROFILE
+            if (lane == 0 && a.prof) prof_idle(a, wc.t_start, w0, globaltimer_ns());
+#endif
             if (!got) break;
         }
         PROF_T0();
@@ -1380,7 +1477,13 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
             uint32_t idx = __shfl_sync(kFull, my_path, j);
             uint32_t nxt = __shfl_sync(kFull, my_path, (j + 1) & 31);
             uint32_t mark = wc.arena_top;
+#ifdef MBE_PROFILE
+            long long c0r = clock64();
+#endif
             ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, wc, acc, true, false);
+#ifdef MBE_PROFILE
+            PROF_TAB(8, c0r, clock64() - c0r);
+#endif
             if (!co.rec) {
                 if (lane == 0) set_error(a, kErrReplay, j);
                 replay_ok = false;
@@ -1423,12 +1526,12 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
                     depth--;
                     continue;
                 }
-                if (donate && (evals & 3u) == 0) {
+                if (donate) {
                     // waiting warps = tickets taken beyond the tasks pushed
                     uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
                     if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) {
                         PROF_T0();
-                        try_donate(a, frames, depth, wc);
+                        try_donate(a, frames, depth, wc, qh - qt);
                         PROF_ADD(wc.prof, kProfDonate);
                     }
                     f = frames[depth];
@@ -1439,7 +1542,13 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
                     PROF_T0();
                     const RecView R = rec_view(nd);
                     uint32_t nb = min(32u, f.end - f.next);
+#ifdef MBE_PROFILE
+                    long long c0p = clock64();
+#endif
                     uint32_t mask = prefilter_w1(R, f.next, nb, acc);
+#ifdef MBE_PROFILE
+                    PROF_TAB(9, c0p, clock64() - c0p);
+#endif
                     PROF_ADD(wc.prof, kProfPrefilter);
                     evals += nb;
                     if (lane == 0) {
@@ -1462,7 +1571,15 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
                 __syncwarp();
             }
             uint32_t mark = wc.arena_top;
+#ifdef MBE_PROFILE
+            long long c0e = clock64();
+            const uint32_t pW = ((const NodeHdr*)f.node)->W;
+#endif
             ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, wc, acc, false, known_max);
+#ifdef MBE_PROFILE
+            PROF_TAB(min(7, 31 - __clz(pW)), c0e, clock64() - c0e);
+            PROF_TAB(10, 0, depth);
+#endif
             evals++;
             if (evals - evals_reported >= 1024) {
                 evals_reported = evals;
@@ -1502,6 +1619,9 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
 #endif
     }
 #ifdef MBE_PROFILE
+    __syncthreads();
+    for (int i = threadIdx.x; i < kProfTB * kProfTC * 2 && a.prof; i += blockDim.x)
+        if (sTab[i]) atomicAdd(&a.prof[kProfSlots + a.prof_warps + 2 * kProfBins + i], sTab[i]);
     if (lane == 0 && a.prof) {
         for (int q = 0; q < kProfSlots; q++) atomicAdd(&a.prof[q], (unsigned long long)wc.prof[q]);
         a.prof[kProfSlots + gw] = wc.last_busy;
@@ -1589,7 +1709,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     bpsm = std::min<uint32_t>(bpsm, (uint32_t)std::max(1, occB));
     uint32_t gridB = (uint32_t)n_sm * bpsm;
     uint32_t nwarpsB = gridB * kWarpsB;
-    const uint32_t q_margin = nwarpsB + 1024;
+    const uint32_t q_margin = 32 * nwarpsB + 1024;  // a donor pushes up to 31 tasks after its check
     const uint32_t task_cap = (uint32_t)std::min<size_t>(roots.size() + q_margin + (size_t)cfg.extra_tasks, 0x7FFFFFFF);
     const uint32_t max_frames = cfg.max_frames;
     // Per-warp DFS arenas default to 4 MiB each (at most 30% of free device
@@ -1637,6 +1757,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.minL = cfg.minL;
     a.minR = cfg.minR;
     a.donate_min = std::max(2u, cfg.donate_min);
+    a.donate_copy = 1;
+    if (const char* e = std::getenv("MBE_DONATE_COPY")) a.donate_copy = (uint32_t)std::atoi(e);
     a.root_next = &ctrl->root_next;
     a.retry = (uint32_t*)eb.retry_in.ptr;
     a.n_retry = &ctrl->n_retry;
@@ -1670,13 +1792,14 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 #ifdef MBE_PROFILE
     static unsigned long long* prof_dev = nullptr;
     static size_t prof_n = 0;
-    if (prof_n < kProfSlots + nwarpsB) {
+    if (prof_n < kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC) {
         if (prof_dev) cudaFree(prof_dev);
-        prof_n = kProfSlots + nwarpsB;
+        prof_n = kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC;
         MBE_CUDA_TRY(cudaMalloc(&prof_dev, sizeof(unsigned long long) * prof_n));
     }
     MBE_CUDA_TRY(cudaMemsetAsync(prof_dev, 0, sizeof(unsigned long long) * prof_n, s));
     a.prof = prof_dev;
+    a.prof_warps = nwarpsB;
 #endif
 
     cudaEvent_t e0, e1, e2;
@@ -1835,6 +1958,32 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         std::fprintf(stderr, "prof warps last busy after the first (ms): p10 %.3f p50 %.3f p90 %.3f p99 %.3f max %.3f\n",
                      (ex[nwarpsB / 10] - t0) / 1e6, (ex[nwarpsB / 2] - t0) / 1e6, (ex[nwarpsB * 9 / 10] - t0) / 1e6,
                      (ex[nwarpsB * 99 / 100] - t0) / 1e6, (ex.back() - t0) / 1e6);
+        std::vector<unsigned long long> hist(2 * kProfBins);
+        MBE_CUDA_TRY(cudaMemcpy(hist.data(), a.prof + kProfSlots + nwarpsB, sizeof(unsigned long long) * 2 * kProfBins,
+                                cudaMemcpyDeviceToHost));
+        std::fprintf(stderr, "prof chunks %u; idle %% of warp time per 20 ms (pops ending):", chunks);
+        for (int b = 0; b < kProfBins; b += 5) {
+            unsigned long long idle = 0, pops = 0;
+            for (int q = b; q < b + 5 && q < kProfBins; q++) idle += hist[q], pops += hist[kProfBins + q];
+            if (!idle && !pops) continue;
+            std::fprintf(stderr, " [%d] %.0f%% (%llu)", b * 4, 100.0 * idle / (5.0 * kProfBinNs * nwarpsB), pops);
+        }
+        std::fprintf(stderr, "\n");
+        std::vector<unsigned long long> tab(2 * kProfTB * kProfTC);
+        MBE_CUDA_TRY(cudaMemcpy(tab.data(), a.prof + kProfSlots + nwarpsB + 2 * kProfBins,
+                                sizeof(unsigned long long) * tab.size(), cudaMemcpyDeviceToHost));
+        std::fprintf(stderr, "prof eval table: per 64 ms, class W1 W2 W4 W8 W16 W32 W64 W128+ replay prefilter: "
+                             "Gcycles/evals; avg depth\n");
+        for (int b = 0; b < kProfTB; b++) {
+            unsigned long long any = 0;
+            for (int c = 0; c < kProfTC; c++) any += tab[(b * kProfTC + c) * 2 + 1];
+            if (!any) continue;
+            std::fprintf(stderr, "  t%4d", b * 64);
+            for (int c = 0; c < 10; c++)
+                std::fprintf(stderr, " %.1f/%llu", tab[(b * kProfTC + c) * 2] / 1e9, tab[(b * kProfTC + c) * 2 + 1]);
+            unsigned long long dn = tab[(b * kProfTC + 10) * 2 + 1];
+            std::fprintf(stderr, " d%.1f\n", dn ? (double)tab[(b * kProfTC + 10) * 2] / dn : 0.0);
+        }
     }
 #endif
     if (stats) {

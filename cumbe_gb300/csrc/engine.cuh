@@ -67,7 +67,12 @@ enum : int {
     kProfExpand,         // expansion (P scan) + hash of maximal children
     kProfBuild,          // child record construction
     kProfSections,
-    kProfSlots = 2 * kProfSections
+    kProfSlots = 2 * kProfSections,
+    kProfBins = 512,           // idle-time histogram over kernel time
+    kProfBinNs = 4000000,      // 4 ms per bin
+    kProfTB = 16,              // eval table: time bins of 64 ms ...
+    kProfTC = 11,              // ... x classes: parent W bucket 0..7, replay, prefilter, depth sum
+    kProfTabNs = 64000000
 };
 
 // A packed record (|L| <= 32) keeps its L bits dense in one word and maps
@@ -118,6 +123,7 @@ struct EngineArgs {
     uint32_t variant;
     uint32_t minL, minR;       // thresholds in L/R orientation (batched: same for all)
     uint32_t donate_min;
+    uint32_t donate_copy;      // 1: donate small arena records by copy into the pool
     // root list: (graph, rank) pairs, processed from index 0
     const uint2* roots;
     uint32_t n_roots;
@@ -159,7 +165,8 @@ struct EngineArgs {
     uint32_t scr_kc;           // key-array capacity (power of two >= scr_n)
     uint32_t max_W;            // largest universe word count
     // section cycle counters (builds with -DMBE_PROFILE only; else null)
-    unsigned long long* prof;  // [kProfSlots]
+    unsigned long long* prof;  // [kProfSlots + warps + 2 * kProfBins]
+    uint32_t prof_warps;
     // results
     ResultAcc* results;        // [n_graphs]
     int* error;
