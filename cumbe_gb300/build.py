@@ -35,6 +35,17 @@ def _flags() -> list[str]:
     # (printed to stderr after each enumeration); off by default.
     if os.environ.get("MBE_PROFILE") == "1":
         f += ["-DMBE_PROFILE"]
+    # MBE_DFS_BLOCKS=N sets the resident blocks per SM the enumeration kernel
+    # is compiled for (its register budget); default 2.
+    if os.environ.get("MBE_DFS_BLOCKS"):
+        f += ["-DMBE_DFS_MIN_BLOCKS=%d" % int(os.environ["MBE_DFS_BLOCKS"])]
+    # MBE_UNROLL=E,G,P sets the scan unroll factors of the enumeration kernel
+    # (expansion chunks, gather chunks, prefilter rows); default 1,1,8.
+    if os.environ.get("MBE_EVAL_NOINLINE") == "1":
+        f += ["-DMBE_EVAL_NOINLINE"]
+    if os.environ.get("MBE_UNROLL"):
+        e, g, p = (int(v) for v in os.environ["MBE_UNROLL"].split(","))
+        f += ["-DMBE_UNROLL_E=%d" % e, "-DMBE_UNROLL_G=%d" % g, "-DMBE_UNROLL_P=%d" % p]
     return f
 
 

@@ -141,7 +141,7 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     const uint32_t scr_n = nR < 32 ? 32 : nR;
     uint32_t kc = 32;
     while (kc < scr_n) kc <<= 1;
-    const size_t sw = ((((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 9 * (size_t)kc) + 31) & ~(size_t)31;
+    const size_t sw = ((((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 6 * (size_t)kc) + 31) & ~(size_t)31;
     const uint32_t q_margin = 32 * kWarps + 1024;  // a donor pushes up to 31 tasks after its check
     const uint32_t task_cap = nR + q_margin + 4096;
 
@@ -188,6 +188,8 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     a.minL = 0;
     a.minR = 0;
     a.donate_min = 2;
+    a.donate_copy = 1;
+    a.solve_rows = 32;
     a.roots = roots;
     a.n_roots = nR;
     a.root_next = &ctrl->root_next;

@@ -37,6 +37,27 @@ constexpr int kThreadsB = kWarpsB * 32;
 constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
 constexpr uint32_t kKeepWindow = 32;     // Q rows a dropped Q row is tested against
+constexpr uint32_t kShRows = 128;        // Q' rows / P' keys of a packed build kept in shared memory
+#ifndef MBE_UNROLL_E
+#define MBE_UNROLL_E 1
+#endif
+#ifndef MBE_UNROLL_G
+#define MBE_UNROLL_G 1
+#endif
+#ifndef MBE_UNROLL_P
+#define MBE_UNROLL_P 8
+#endif
+constexpr int kUnrollE = MBE_UNROLL_E;   // 32-row chunks in flight per step of the expansion scan
+constexpr int kUnrollG = MBE_UNROLL_G;   // ... of the Q' gather of a packed build
+constexpr int kUnrollP = MBE_UNROLL_P;   // rows in flight per lane in the batch prefilter
+constexpr uint32_t kSolveRows = 32;      // packed records with at most this many rows are solved in registers
+
+// One saved level of the register-resident small-record search (row masks
+// over the record's rows, one row per lane).
+struct SolveLevel {
+    uint32_t L, Q, P, pend, nR, pad;
+    unsigned long long sR;
+};
 constexpr uint32_t kDonateSlabMax = 8192;      // arena records up to this size are copied into a slab
 constexpr uint32_t kDonateCopyMax = 1u << 20;  // larger ones up to this size by a direct pool allocation
 constexpr uint32_t kSlabWords = 1u << 16;      // pool slab a warp takes for donation copies
@@ -92,10 +113,12 @@ __device__ bool push_task(const EngineArgs& a, Task t) {
         }                                                                                                 \
     } while (0)
 #define PROF_T0() long long prof_t0__ = clock64()
+#define PROF_VAL(acc_arr, sec, v) do { (acc_arr)[2 * (sec)] += (v); (acc_arr)[2 * (sec) + 1]++; } while (0)
 #define PROF_ADD(acc_arr, sec) do { (acc_arr)[2 * (sec)] += clock64() - prof_t0__; (acc_arr)[2 * (sec) + 1]++; prof_t0__ = clock64(); } while (0)
 #else
 #define PROF_T0() do {} while (0)
 #define PROF_ADD(acc_arr, sec) do {} while (0)
+#define PROF_VAL(acc_arr, sec, v) do {} while (0)
 #define PROF_TAB(cls, c0, v) do {} while (0)
 #endif
 
@@ -561,8 +584,12 @@ struct WarpCtx {
     unsigned long long* scrKeysQ;
     uint32_t* sLi;
     uint32_t* sNz;
-    uint32_t* scrPack;     // 5 x kc words: qrow, qpos, srow, spos, porder
-    uint32_t* sBucket;     // 32 words of shared memory
+    uint32_t* scrPack;     // 2 x kc words: srow, spos of a packed build too large for shared memory
+    uint32_t* sBucket;     // 64 words of shared memory: Q' then P' count buckets
+    uint32_t* shRow;       // kShRows Q' rows of a packed build (shared memory)
+    uint32_t* shPos;       // their parent positions
+    unsigned long long* shKeys;  // kShRows P' keys of a packed child (shared memory)
+    SolveLevel* solve;     // kSolveRows + 1 saved levels (shared memory)
     unsigned long long slab_off, slab_end;  // this warp's slab of the node pool (donation copies)
 #ifdef MBE_PROFILE
     long long prof[kProfSlots];
@@ -683,44 +710,6 @@ __device__ __forceinline__ uint32_t pext32(uint32_t x, uint32_t m) {
     return r;
 }
 
-// Stable counting sort by a small key (< 32) within a warp: keys are
-// produced by key_of(i) for items 0..n-1 in order; the item index of every
-// output position is written to out[].  Buckets live in shared memory; items
-// with equal keys keep their input order.
-template <typename KeyOf>
-__device__ void warp_bucket_sort(uint32_t n, KeyOf key_of, uint32_t* out, uint32_t* sb) {
-    const unsigned lane = lane_id();
-    sb[lane] = 0;
-    __syncwarp();
-    for (uint32_t base = 0; base < n; base += 32) {
-        uint32_t i = base + lane;
-        bool v = i < n;
-        uint32_t key = v ? key_of(i) : 32u;
-        unsigned grp = __match_any_sync(kFull, key);
-        if (v && (grp & lanemask_lt()) == 0) atomicAdd(&sb[key], __popc(grp));
-    }
-    __syncwarp();
-    uint32_t cnt = sb[lane], ex = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(kFull, ex, o);
-        if (lane >= (unsigned)o) ex += y;
-    }
-    __syncwarp();
-    sb[lane] = ex - cnt;  // exclusive offsets
-    __syncwarp();
-    for (uint32_t base = 0; base < n; base += 32) {
-        uint32_t i = base + lane;
-        bool v = i < n;
-        uint32_t key = v ? key_of(i) : 32u;
-        unsigned grp = __match_any_sync(kFull, key);
-        uint32_t off = v ? sb[key] : 0u;
-        if (v) out[off + __popc(grp & lanemask_lt())] = i;
-        __syncwarp();
-        if (v && (grp & lanemask_lt()) == 0) sb[key] = off + __popc(grp);
-        __syncwarp();
-    }
-}
 
 // Bit compress with a fixed mask (Warren, Hacker's Delight, 2nd ed., 7-4):
 // the five shift masks depend on the mask only, so a build that packs many
@@ -773,56 +762,105 @@ __device__ __forceinline__ uint32_t packed_row(const uint32_t* M, uint32_t n, co
     return row;
 }
 
-// Child record construction when |L_i| <= 32: rows are packed to one word
-// first, so ordering is a counting sort over at most 31 counts and the Q
-// reduction compares single words held in lane registers.  Produces the
-// same record (same order, same reduction) as the general path would with
-// packed rows.
+// Position of the k-th (0-based) set bit of x (k < popc(x)), by halving.
+__device__ __forceinline__ uint32_t select32(uint32_t x, uint32_t k) {
+    uint32_t pos = 0, c;
+    c = __popc(x & 0xFFFFu);
+    if (k >= c) { k -= c; x >>= 16; pos += 16; }
+    c = __popc(x & 0xFFu);
+    if (k >= c) { k -= c; x >>= 8; pos += 8; }
+    c = __popc(x & 0xFu);
+    if (k >= c) { k -= c; x >>= 4; pos += 4; }
+    c = __popc(x & 0x3u);
+    if (k >= c) { k -= c; x >>= 2; pos += 2; }
+    if (k >= (x & 1u)) pos += 1;
+    return pos;
+}
+
+// Turns per-key counts sb[0..32) into exclusive offsets; returns the total.
+__device__ __forceinline__ uint32_t bucket_offsets(uint32_t* sb) {
+    const unsigned lane = lane_id();
+    __syncwarp();
+    uint32_t cnt = sb[lane], inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= (unsigned)o) inc += y;
+    }
+    __syncwarp();
+    sb[lane] = inc - cnt;
+    __syncwarp();
+    return __shfl_sync(kFull, inc, 31);
+}
+
+// Child record construction when |L_i| <= 32: rows are packed to one word,
+// so ordering is a counting sort over at most 31 counts and the Q reduction
+// compares single words held in lane registers.  The Q' rows are gathered
+// twice (a count histogram, then a scatter straight to their sorted slots,
+// in shared memory when they fit); the P' histogram was taken during the
+// expansion scan, so P' rows are written straight to their record slots.
+// Produces the same record (same order, same reduction) as the general
+// path would with packed rows.
 __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const NodeHdr* h, uint32_t xi, uint32_t li,
                                  uint32_t nnz, const uint32_t* Li, const uint32_t* Nz, uint32_t npp, uint32_t nR2,
-                                 unsigned long long sR2, WarpCtx& wc, ResultAcc& acc) {
+                                 unsigned long long sR2, const unsigned long long* keysP, const GraphView& G,
+                                 WarpCtx& wc, ResultAcc& acc) {
     const unsigned lane = lane_id();
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t* M = R.M;
-    const uint32_t kc = a.scr_kc;
-    uint32_t* qrow = wc.scrPack;
-    uint32_t* qpos = qrow + kc;
-    uint32_t* srow = qpos + kc;
-    uint32_t* spos = srow + kc;
-    uint32_t* porder = spos + kc;
     const CompressPlan plan0 = compress_plan(Li[0]);
     ChildOut out{nullptr, 0, 0};
-    // Q' = rows of Q u P[0..i) meeting L_i, packed, in parent order
-    uint32_t m = 0;
-    for (uint32_t base = 0; base < xi; base += 128) {  // four chunks per step: independent loads
-        uint32_t r[4];
+    PROF_T0();
+    // Q' = rows of Q u P[0..i) meeting L_i, by count descending (key li -
+    // count in 1..31), parent order within a count
+    uint32_t* sb = wc.sBucket;
+    sb[lane] = 0;
+    __syncwarp();
+    for (uint32_t base = 0; base < xi; base += 32 * kUnrollG) {  // kUnrollG chunks per step: independent loads
+        uint32_t r[kUnrollG];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < kUnrollG; q++) {
             uint32_t c = base + 32 * q + lane;
             r[q] = c < xi ? packed_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            unsigned b = __ballot_sync(kFull, r[q] != 0);
-            if (r[q]) {
-                uint32_t p = m + __popc(b & lanemask_lt());
-                qrow[p] = r[q];
-                qpos[p] = base + 32 * q + lane;
-            }
-            m += __popc(b);
+        for (int q = 0; q < kUnrollG; q++) {
+            if (base + 32 * q >= xi) break;  // uniform: no rows left
+            uint32_t key = r[q] ? li - __popc(r[q]) : 32u;
+            unsigned grp = __match_any_sync(kFull, key);
+            if (r[q] && (grp & lanemask_lt()) == 0) atomicAdd(&sb[key], (uint32_t)__popc(grp));
         }
     }
-    __syncwarp();
-    acc.words += (unsigned long long)xi * nnz;
-    // count descending (key li - count in 1..31), parent order within a count
-    warp_bucket_sort(m, [&](uint32_t i) { return li - __popc(qrow[i]); }, porder, wc.sBucket);
-    __syncwarp();
-    for (uint32_t t = lane; t < m; t += 32) {
-        uint32_t i = porder[t];
-        srow[t] = qrow[i];
-        spos[t] = qpos[i];
+    const uint32_t m = bucket_offsets(sb);
+    const bool shq = m <= kShRows;
+    uint32_t* srow = shq ? wc.shRow : wc.scrPack;
+    uint32_t* spos = shq ? wc.shPos : wc.scrPack + a.scr_kc;
+    for (uint32_t base = 0; base < xi; base += 32 * kUnrollG) {
+        uint32_t r[kUnrollG];
+#pragma unroll
+        for (int q = 0; q < kUnrollG; q++) {
+            uint32_t c = base + 32 * q + lane;
+            r[q] = c < xi ? packed_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < kUnrollG; q++) {
+            if (base + 32 * q >= xi) break;  // uniform: no rows left
+            uint32_t key = r[q] ? li - __popc(r[q]) : 32u;
+            unsigned grp = __match_any_sync(kFull, key);
+            uint32_t off = r[q] ? sb[key] : 0u;
+            if (r[q]) {
+                uint32_t p = off + __popc(grp & lanemask_lt());
+                srow[p] = r[q];
+                spos[p] = base + 32 * q + lane;
+            }
+            __syncwarp();
+            if (r[q] && (grp & lanemask_lt()) == 0) sb[key] = off + __popc(grp);
+            __syncwarp();
+        }
     }
-    __syncwarp();
+    acc.words += (unsigned long long)xi * nnz;
+    PROF_ADD(wc.prof, kProfBGather);
+    PROF_ADD(wc.prof, kProfBSort);
     // reduction, 32 candidates per step: every lane tests its row against the
     // window (the first kKeepWindow kept rows, in lane registers); the
     // survivors are then taken in order, and each one that joins the window
@@ -859,9 +897,10 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
         nq2 += __popc(keep);
         __syncwarp();
     }
+    PROF_ADD(wc.prof, kProfBReduce);
     // P' by count ascending, parent order within a count (keys in scan order)
-    warp_bucket_sort(npp, [&](uint32_t t) { return (uint32_t)(wc.scrKeysP[t] >> 32); }, porder, wc.sBucket);
-    __syncwarp();
+    uint32_t* sbp = wc.sBucket + 32;
+    bucket_offsets(sbp);
     // allocate and write
     const uint32_t n2 = nq2 + npp;
     const uint64_t rw = record_words(1, n2, true);
@@ -901,175 +940,74 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
         h2->flags = kRecPacked;
         Lm2[0] = li == 32 ? 0xFFFFFFFFu : ((1u << li) - 1u);
     }
-    // lane t < li: root bit of the t-th set bit of L_i (words in order)
+    // lane t < li: L vertex of the t-th set bit of L_i (words in order)
     if (lane < li) {
-        const bool parent_packed = (R.flags & kRecPacked) != 0;
-        uint32_t before = 0, rootbit = 0;
-        for (uint32_t k = 0; k < nnz; k++) {
-            uint32_t c = __popc(Li[k]);
-            if (lane < before + c) {
-                uint32_t bits = Li[k];
-                for (uint32_t s = before; s < lane; s++) bits &= bits - 1;
-                uint32_t b = __ffs(bits) - 1;
-                rootbit = parent_packed ? R.map[b] : R.map[Nz[k]] * 32 + b;
-                break;
+        uint32_t vtx;
+        if (R.flags & kRecPacked) {
+            vtx = R.map[select32(Li[0], lane)];
+        } else {
+            uint32_t before = 0, k = 0;
+            for (; k + 1 < nnz; k++) {
+                uint32_t c = __popc(Li[k]);
+                if (lane < before + c) break;
+                before += c;
             }
-            before += c;
+            const uint32_t* L0 = G.r_adj + G.r_ptr[h->root];
+            vtx = L0[R.map[Nz[k]] * 32 + select32(Li[k], lane - before)];
         }
-        map2[lane] = rootbit;
+        map2[lane] = vtx;
     }
     for (uint32_t t = lane; t < nq2; t += 32) {
         cand2[t] = R.cand[spos[t]];
         cnt2[t] = 0;
         M2[t] = srow[t];
     }
-    for (uint32_t t = lane; t < npp; t += 32) {
-        unsigned long long key = wc.scrKeysP[porder[t]];
-        uint32_t c = nq + (uint32_t)key;
-        cand2[nq2 + t] = R.cand[c];
-        cnt2[nq2 + t] = (uint32_t)(key >> 32);
-        M2[nq2 + t] = packed_row(M, n, Nz, Li, nnz, c, plan0);
+    for (uint32_t base = 0; base < npp; base += 32) {
+        uint32_t t = base + lane;
+        bool v = t < npp;
+        unsigned long long key = v ? keysP[t] : 0ull;
+        uint32_t cc = v ? (uint32_t)(key >> 32) : 32u;
+        unsigned grp = __match_any_sync(kFull, cc);
+        uint32_t off = v ? sbp[cc] : 0u;
+        if (v) {
+            uint32_t dst = nq2 + off + __popc(grp & lanemask_lt());
+            uint32_t c = nq + (uint32_t)key;
+            cand2[dst] = R.cand[c];
+            cnt2[dst] = cc;
+            M2[dst] = packed_row(M, n, Nz, Li, nnz, c, plan0);
+        }
+        __syncwarp();
+        if (v && (grp & lanemask_lt()) == 0) sbp[cc] = off + __popc(grp);
+        __syncwarp();
     }
     acc.words += (unsigned long long)n2 + (unsigned long long)npp * nnz;
     __syncwarp();
+    PROF_ADD(wc.prof, kProfBWrite);
+    PROF_VAL(wc.prof, kProfSumXi, xi);
+    PROF_VAL(wc.prof, kProfSumM, m);
+    PROF_VAL(wc.prof, kProfSumNq2, nq2);
+    PROF_VAL(wc.prof, kProfSumNpp, npp);
     out.rec = rec;
     out.nchild = npp;
     return out;
 }
 
-// Evaluates child i of the node record `nd` (one tree node).  Counts and
-// hashes the biclique when maximal; materialises the child record when it
-// has candidates.  Warp-collective.  known_max: the caller has already
-// established that no row of Q u P[0..i) covers L_i (batch prefilter).
-//
-// The child's Q part is ordered by |N(v) n L_i| descending and reduced:
-// a Q row contained in one of the first kKeepWindow kept rows is dropped,
-// since whatever it covers in the subtree the containing row covers too.
-// Large rows first make the first covering row of a non-maximal
-// descendant appear within the first few candidates.  A child with
-// |L_i| <= 32 is written packed: one word per row, L bits dense.
-__device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, WarpCtx& wc,
-                               ResultAcc& acc_out, bool replay, bool known_max) {
-    // a replayed evaluation re-derives a donated node: its counts belong to
-    // the donor and are discarded
-    ResultAcc scratch_acc{};
-    ResultAcc& acc = replay ? scratch_acc : acc_out;
+// Child record construction when |L_i| > 32 (rows stay word-sliced): the
+// Q part is sorted by count descending and reduced against a window of kept
+// rows, the P part sorted by count ascending.  Kept out of line: it is rare
+// next to packed builds and large.
+__device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
+                                               uint32_t xi, uint32_t li, uint32_t nnz, const uint32_t* Li,
+                                               const uint32_t* Nz, uint32_t npp, uint32_t nR2,
+                                               unsigned long long sR2, bool known_max, WarpCtx& wc, ResultAcc& acc) {
     const unsigned lane = lane_id();
     PROF_T0();
     const NodeHdr* h = (const NodeHdr*)nd;
     const RecView R = rec_view(nd);
-    const uint32_t W = R.W, n = R.n, nq = R.nq;
-    const bool packed = (R.flags & kRecPacked) != 0;
+    const uint32_t n = R.n, nq = R.nq;
     const uint32_t* M = R.M;
     const uint32_t* cand = R.cand;
-    const uint32_t xi = nq + i;
-    const uint32_t li = R.cnt[xi];
-    uint32_t* Li = W <= kSmemW ? wc.sLi : wc.scrLi;
-    uint32_t* Nz = W <= kSmemW ? wc.sNz : wc.scrNz;
     ChildOut out{nullptr, 0, 0};
-
-    // 1. L_i = L n N(x_i), keeping only non-zero words
-    uint32_t nnz = 0;
-    for (uint32_t base = 0; base < W; base += 32) {
-        uint32_t w = base + lane;
-        uint32_t v = w < W ? (R.Lm[w] & M[(size_t)w * n + xi]) : 0u;
-        unsigned bal = __ballot_sync(kFull, v != 0);
-        if (v) {
-            uint32_t pos = nnz + __popc(bal & lanemask_lt());
-            Li[pos] = v;
-            Nz[pos] = w;
-        }
-        nnz += __popc(bal);
-    }
-    __syncwarp();
-    if (!known_max) acc.nodes++;
-    acc.words += W;
-
-    // 2. maximality against Q u P[0..i); counts kept for Q'
-    if (!known_max) {
-        const bool es = a.variant != MBE_NOES;
-        bool maximal = true;
-        for (uint32_t base = 0; base < xi; base += 32) {
-            uint32_t c = base + lane;
-            uint32_t cc = 0;
-            if (c < xi) {
-                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
-                wc.scrQcnt[c] = cc;
-            }
-            unsigned full = __ballot_sync(kFull, c < xi && cc == li);
-            acc.words += (unsigned long long)nnz * min(32u, xi - base);
-            if (full) {
-                maximal = false;
-                if (es) break;
-            }
-        }
-        __syncwarp();
-        PROF_ADD(wc.prof, kProfQscan);
-        if (!maximal) return out;
-    }
-
-    // 3. expansion over P(i..], two chunks per step (independent loads)
-    uint32_t npp = 0, nabs = 0;
-    unsigned long long sabs = 0;
-    for (uint32_t base = xi + 1; base < n; base += 64) {
-        uint32_t cc2[2];
-#pragma unroll
-        for (int h2 = 0; h2 < 2; h2++) {
-            uint32_t c = base + 32 * h2 + lane;
-            uint32_t cc = 0;
-            if (c < n)
-                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
-            cc2[h2] = cc;
-        }
-#pragma unroll
-        for (int h2 = 0; h2 < 2; h2++) {
-            uint32_t c = base + 32 * h2 + lane;
-            bool valid = c < n;
-            uint32_t cc = cc2[h2];
-            bool absorbed = valid && cc == li;
-            bool partial = valid && cc > 0 && cc < li;
-            if (absorbed) sabs += G.eR[cand[c]];
-            unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
-            if (partial) wc.scrKeysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
-            npp += __popc(pb);
-            nabs += __popc(ab);
-        }
-        acc.words += (unsigned long long)nnz * min(64u, n - base);
-    }
-    __syncwarp();
-    sabs = warp_sum(sabs);
-    const uint32_t nR2 = h->nRset + 1 + nabs;
-    const unsigned long long sR2 = h->sR + G.eR[cand[xi]] + sabs;
-
-    // 4. count + canonical hash
-    if (li >= a.minL && nR2 >= a.minR) {
-        const uint32_t* L0 = G.r_adj + G.r_ptr[h->root];
-        unsigned long long sl = 0;
-        if (packed) {
-            if ((Li[0] >> lane) & 1u) sl = G.eL[L0[R.map[lane]]];
-        } else {
-            for (uint32_t k = lane; k < nnz; k += 32) {
-                uint32_t bits = Li[k], b0 = R.map[Nz[k]] * 32;
-                while (bits) {
-                    uint32_t t = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    sl += G.eL[L0[b0 + t]];
-                }
-            }
-        }
-        sl = warp_sum(sl);
-        acc.count++;
-        acc.hash += side_hash(G, sl, li, sR2, nR2);
-    }
-
-    // 5. child record
-    PROF_ADD(wc.prof, kProfExpand);
-    if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
-    if (li <= 32) {
-        out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, wc, acc);
-        PROF_ADD(wc.prof, kProfBuild);
-        return out;
-    }
     if (known_max) {
         // the prefilter only settled maximality: count Q u P[0..i) now
         for (uint32_t base = 0; base < xi; base += 32) {
@@ -1151,9 +1089,8 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
     __syncwarp();
 
     // 5d. allocate and write the record
-    const bool packed2 = li <= 32;
-    const uint32_t n2 = nq2 + npp, W2 = packed2 ? 1u : nnz;
-    const uint64_t rw = record_words(W2, n2, packed2);
+    const uint32_t n2 = nq2 + npp, W2 = nnz;  // |L_i| > 32 here: an unpacked child
+    const uint64_t rw = record_words(W2, n2, false);
     uint32_t* rec;
     if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
         rec = wc.arena + wc.arena_top;
@@ -1170,7 +1107,7 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         out.size = 0;
     }
     uint32_t* map2 = rec + kHdrWords;
-    uint32_t* Lm2 = map2 + (packed2 ? 32u : pad4(W2));
+    uint32_t* Lm2 = map2 + pad4(W2);
     uint32_t* cand2 = Lm2 + pad4(W2);
     uint32_t* cnt2 = cand2 + pad4(n2);
     uint32_t* M2 = cnt2 + pad4(n2);
@@ -1187,31 +1124,11 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         h2->sR = sR2;
         h2->words = (uint32_t)rw;
         h2->rlist = 0;
-        h2->flags = packed2 ? kRecPacked : 0u;
+        h2->flags = 0u;
     }
-    if (packed2) {
-        // lane t < li: root bit of the t-th set bit of L_i (words in order)
-        if (lane < li) {
-            uint32_t before = 0, rootbit = 0;
-            for (uint32_t k = 0; k < nnz; k++) {
-                uint32_t c = __popc(Li[k]);
-                if (lane < before + c) {
-                    uint32_t bits = Li[k];
-                    for (uint32_t s = before; s < lane; s++) bits &= bits - 1;
-                    uint32_t b = __ffs(bits) - 1;
-                    rootbit = packed ? R.map[b] : R.map[Nz[k]] * 32 + b;
-                    break;
-                }
-                before += c;
-            }
-            map2[lane] = rootbit;
-        }
-        if (lane == 0) Lm2[0] = li == 32 ? 0xFFFFFFFFu : ((1u << li) - 1u);
-    } else {
-        for (uint32_t k = lane; k < W2; k += 32) {
-            map2[k] = R.map[Nz[k]];
-            Lm2[k] = Li[k];
-        }
+    for (uint32_t k = lane; k < W2; k += 32) {
+        map2[k] = R.map[Nz[k]];
+        Lm2[k] = Li[k];
     }
     for (uint32_t t = lane; t < n2; t += 32) {
         uint32_t c, cntv;
@@ -1225,22 +1142,166 @@ __device__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const ui
         }
         cand2[t] = cand[c];
         cnt2[t] = cntv;
-        if (packed2) {
-            uint32_t row = 0, sh = 0;
-            for (uint32_t k = 0; k < nnz; k++) {
-                row |= pext32(M[(size_t)Nz[k] * n + c], Li[k]) << sh;
-                sh += __popc(Li[k]);
-            }
-            M2[t] = row;
-        } else {
-            for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + t] = M[(size_t)Nz[k] * n + c] & Li[k];
-        }
+        for (uint32_t k = 0; k < W2; k++) M2[(size_t)k * n2 + t] = M[(size_t)Nz[k] * n + c] & Li[k];
     }
     acc.words += (unsigned long long)W2 * n2;
     __syncwarp();
     PROF_ADD(wc.prof, kProfBuild);
     out.rec = rec;
     out.nchild = npp;
+    return out;
+}
+
+// Evaluates child i of the node record `nd` (one tree node).  Counts and
+// hashes the biclique when maximal; materialises the child record when it
+// has candidates.  Warp-collective.  known_max: the caller has already
+// established that no row of Q u P[0..i) covers L_i (batch prefilter).
+//
+// The child's Q part is ordered by |N(v) n L_i| descending and reduced:
+// a Q row contained in one of the first kKeepWindow kept rows is dropped,
+// since whatever it covers in the subtree the containing row covers too.
+// Large rows first make the first covering row of a non-maximal
+// descendant appear within the first few candidates.  A child with
+// |L_i| <= 32 is written packed: one word per row, L bits dense.
+#ifdef MBE_EVAL_NOINLINE
+__device__ __noinline__
+#else
+__device__
+#endif
+ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, WarpCtx& wc,
+                               ResultAcc& acc_out, bool replay, bool known_max) {
+    // a replayed evaluation re-derives a donated node: its counts belong to
+    // the donor and are discarded
+    ResultAcc scratch_acc{};
+    ResultAcc& acc = replay ? scratch_acc : acc_out;
+    const unsigned lane = lane_id();
+    PROF_T0();
+    const NodeHdr* h = (const NodeHdr*)nd;
+    const RecView R = rec_view(nd);
+    const uint32_t W = R.W, n = R.n, nq = R.nq;
+    const bool packed = (R.flags & kRecPacked) != 0;
+    const uint32_t* M = R.M;
+    const uint32_t* cand = R.cand;
+    const uint32_t xi = nq + i;
+    const uint32_t li = R.cnt[xi];
+    uint32_t* Li = W <= kSmemW ? wc.sLi : wc.scrLi;
+    uint32_t* Nz = W <= kSmemW ? wc.sNz : wc.scrNz;
+    ChildOut out{nullptr, 0, 0};
+
+    // 1. L_i = L n N(x_i), keeping only non-zero words
+    uint32_t nnz = 0;
+    for (uint32_t base = 0; base < W; base += 32) {
+        uint32_t w = base + lane;
+        uint32_t v = w < W ? (R.Lm[w] & M[(size_t)w * n + xi]) : 0u;
+        unsigned bal = __ballot_sync(kFull, v != 0);
+        if (v) {
+            uint32_t pos = nnz + __popc(bal & lanemask_lt());
+            Li[pos] = v;
+            Nz[pos] = w;
+        }
+        nnz += __popc(bal);
+    }
+    __syncwarp();
+    if (!known_max) acc.nodes++;
+    acc.words += W;
+
+    // 2. maximality against Q u P[0..i); counts kept for Q'
+    if (!known_max) {
+        const bool es = a.variant != MBE_NOES;
+        bool maximal = true;
+        for (uint32_t base = 0; base < xi; base += 32) {
+            uint32_t c = base + lane;
+            uint32_t cc = 0;
+            if (c < xi) {
+                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+                wc.scrQcnt[c] = cc;
+            }
+            unsigned full = __ballot_sync(kFull, c < xi && cc == li);
+            acc.words += (unsigned long long)nnz * min(32u, xi - base);
+            if (full) {
+                maximal = false;
+                if (es) break;
+            }
+        }
+        __syncwarp();
+        PROF_ADD(wc.prof, kProfQscan);
+        if (!maximal) return out;
+    }
+
+    // 3. expansion over P(i..], two chunks per step (independent loads).
+    // For a packed child (|L_i| <= 32) the P' count histogram is taken here
+    // and the keys stay in shared memory when they fit.
+    const bool packed_child = li <= 32;
+    unsigned long long* keysP = packed_child && n - xi - 1 <= kShRows ? wc.shKeys : wc.scrKeysP;
+    if (packed_child) wc.sBucket[32 + lane] = 0;
+    __syncwarp();
+    uint32_t npp = 0, nabs = 0;
+    unsigned long long sabs = 0;
+    for (uint32_t base = xi + 1; base < n; base += 32 * kUnrollE) {
+        uint32_t cc2[kUnrollE];
+#pragma unroll
+        for (int h2 = 0; h2 < kUnrollE; h2++) {
+            uint32_t c = base + 32 * h2 + lane;
+            uint32_t cc = 0;
+            if (c < n)
+                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+            cc2[h2] = cc;
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < kUnrollE; h2++) {
+            if (base + 32 * h2 >= n) break;  // uniform: no rows left
+            uint32_t c = base + 32 * h2 + lane;
+            bool valid = c < n;
+            uint32_t cc = cc2[h2];
+            bool absorbed = valid && cc == li;
+            bool partial = valid && cc > 0 && cc < li;
+            if (absorbed) sabs += G.eR[cand[c]];
+            unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
+            if (partial) keysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
+            if (packed_child && pb) {
+                unsigned grp = __match_any_sync(kFull, partial ? cc : 32u);
+                if (partial && (grp & lanemask_lt()) == 0) atomicAdd(&wc.sBucket[32 + cc], (uint32_t)__popc(grp));
+            }
+            npp += __popc(pb);
+            nabs += __popc(ab);
+        }
+        acc.words += (unsigned long long)nnz * min(32u * kUnrollE, n - base);
+    }
+    __syncwarp();
+    sabs = warp_sum(sabs);
+    const uint32_t nR2 = h->nRset + 1 + nabs;
+    const unsigned long long sR2 = h->sR + G.eR[cand[xi]] + sabs;
+
+    // 4. count + canonical hash
+    if (li >= a.minL && nR2 >= a.minR) {
+        unsigned long long sl = 0;
+        if (packed) {
+            if ((Li[0] >> lane) & 1u) sl = G.eL[R.map[lane]];  // packed maps hold L vertices
+        } else {
+            const uint32_t* L0 = G.r_adj + G.r_ptr[h->root];
+            for (uint32_t k = lane; k < nnz; k += 32) {
+                uint32_t bits = Li[k], b0 = R.map[Nz[k]] * 32;
+                while (bits) {
+                    uint32_t t = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    sl += G.eL[L0[b0 + t]];
+                }
+            }
+        }
+        sl = warp_sum(sl);
+        acc.count++;
+        acc.hash += side_hash(G, sl, li, sR2, nR2);
+    }
+
+    // 5. child record
+    PROF_ADD(wc.prof, kProfExpand);
+    if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
+    if (packed_child) {
+        out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, keysP, G, wc, acc);
+        PROF_ADD(wc.prof, kProfBuild);
+        return out;
+    }
+    out = build_general(a, G, nd, xi, li, nnz, Li, Nz, npp, nR2, sR2, known_max, wc, acc);
     return out;
 }
 
@@ -1259,14 +1320,14 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, R
     uint32_t c = 0;
     while (__any_sync(kFull, !covered && c < lim)) {
 #pragma unroll
-        for (uint32_t u = 0; u < 8; u++) {
+        for (uint32_t u = 0; u < (uint32_t)kUnrollP; u++) {
             uint32_t cc = c + u;
             if (!covered && cc < lim) {
                 uint32_t r = R.M[cc];
                 covered = (r & Li) == Li;
             }
         }
-        c += 8;
+        c += kUnrollP;
     }
     unsigned long long scanned = active ? min(c, lim) : 0u;
     scanned = warp_sum(scanned);
@@ -1386,6 +1447,133 @@ __device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, Resu
     acc = ResultAcc{};
 }
 
+// Children (lanes in `kids`) of a small-record node (L, Q, P) that no row of
+// Q, nor an earlier row of P, covers: one lane per child, the coverers taken
+// in row order with their rows broadcast by shuffle.  Warp-collective.
+__device__ __forceinline__ uint32_t solve_maximal(uint32_t row, uint32_t L, uint32_t Q, uint32_t P, uint32_t kids) {
+    const unsigned lane = lane_id();
+    const uint32_t Lx = L & row;
+    const bool mine = (kids >> lane) & 1u;
+    const uint32_t last = 31u - __clz(kids);
+    // P rows at or after the last child cover nothing (Q rows precede all of P)
+    uint32_t J = Q | (P & ((1u << last) - 1u));
+    bool covered = false;
+    for (uint32_t it = 1; J; it++) {
+        const uint32_t j = __ffs(J) - 1;
+        J &= J - 1;
+        const uint32_t rj = __shfl_sync(kFull, row, j);
+        const bool elig = ((Q >> j) & 1u) || j < lane;
+        covered = covered || (mine && elig && (rj & Lx) == Lx);
+        if ((it & 7u) == 0 && !__any_sync(kFull, mine && !covered)) break;
+    }
+    return __ballot_sync(kFull, mine && !covered);
+}
+
+// Enumerates the subtree below the children [next, end) of frame `fdepth`,
+// whose record is packed with at most kSolveRows rows, without building
+// child records: lane j holds row j (a mask over the record's L bits), and
+// a tree node is (L, Q, P) with Q and P masks over the lanes.  Child x of a
+// node takes L' = L & row_x; rows of P after x meeting all of L' join R,
+// those meeting part of it form P', rows of Q or of P before x meeting it
+// form Q'.  Rows are never reduced, so every check is one pass of shuffles.
+// Q rows always precede the children of their node in row order.  The
+// frame mirrors level 0 (next = one past the child in progress), so a donor
+// may split the remaining level-0 children off as an ordinary task; the
+// search then drops those it no longer owns.  Warp-collective.
+__device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G, const uint32_t* nd, Frame* frames,
+                                         int fdepth, WarpCtx& wc, ResultAcc& acc, bool donate) {
+    const unsigned lane = lane_id();
+    const NodeHdr* h = (const NodeHdr*)nd;
+    const RecView R = rec_view(nd);
+    const uint32_t n = R.n, nq = R.nq;
+    const uint32_t row = lane < n ? R.M[lane] : 0u;
+    const unsigned long long eR = lane < n ? G.eR[R.cand[lane]] : 0ull;
+    const uint32_t Lroot = R.Lm[0];
+    const unsigned long long eL = ((Lroot >> lane) & 1u) ? G.eL[R.map[lane]] : 0ull;  // packed maps hold L vertices
+    SolveLevel* st = wc.solve;
+    const uint32_t all = n >= 32 ? ~0u : ((1u << n) - 1u);
+    const uint32_t Qroot = (1u << nq) - 1u;  // nq < n <= 32
+    const uint32_t lo = nq + frames[fdepth].next, hi = nq + frames[fdepth].end;
+    const uint32_t kids0 = (hi >= 32 ? ~0u : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+    uint32_t L = Lroot, Q = Qroot, P = all & ~Qroot, nR = h->nRset;
+    unsigned long long sR = h->sR;
+    uint32_t pend = solve_maximal(row, L, Q, P, kids0);
+    acc.nodes += __popc(kids0);
+    acc.words += n + 32;
+    int depth = 0;
+    uint32_t iter = 0;
+    for (;;) {
+        if (pend == 0) {
+            if (depth == 0) break;
+            depth--;
+            const SolveLevel sv = st[depth];
+            L = sv.L;
+            Q = sv.Q;
+            P = sv.P;
+            pend = sv.pend;
+            nR = sv.nR;
+            sR = sv.sR;
+            continue;
+        }
+        const uint32_t x = __ffs(pend) - 1;
+        pend &= pend - 1;
+        if (depth == 0 && lane == 0) {
+            frames[fdepth].next = x - nq + 1;
+            frames[fdepth].cur = x - nq;
+        }
+        const uint32_t L2 = L & __shfl_sync(kFull, row, x);
+        const uint32_t l2 = __popc(L2);
+        const uint32_t c = __popc(row & L2);
+        const bool inA = ((P >> lane) & 1u) && lane > x;
+        const bool inQ = ((Q >> lane) & 1u) || (((P >> lane) & 1u) && lane < x);
+        const uint32_t absorbed = __ballot_sync(kFull, inA && c == l2);
+        const uint32_t P2 = __ballot_sync(kFull, inA && c > 0 && c < l2);
+        const uint32_t Q2 = __ballot_sync(kFull, inQ && c > 0);
+        const uint32_t nR2 = nR + 1 + __popc(absorbed);
+        unsigned long long sR2 = sR + __shfl_sync(kFull, eR, x);
+        if (absorbed) sR2 += warp_sum(((absorbed >> lane) & 1u) ? eR : 0ull);
+        if (l2 >= a.minL && nR2 >= a.minR) {
+            const unsigned long long sl = warp_sum(((L2 >> lane) & 1u) ? eL : 0ull);
+            acc.count++;
+            acc.hash += side_hash(G, sl, l2, sR2, nR2);
+        }
+        if (P2 && l2 >= a.minL && nR2 + __popc(P2) >= a.minR) {
+            const uint32_t pend2 = solve_maximal(row, L2, Q2, P2, P2);
+            acc.nodes += __popc(P2);
+            if (pend2) {
+                if (lane == 0) st[depth] = SolveLevel{L, Q, P, pend, nR, 0u, sR};
+                __syncwarp();
+                depth++;
+                L = L2;
+                Q = Q2;
+                P = P2;
+                pend = pend2;
+                nR = nR2;
+                sR = sR2;
+            }
+        }
+        if ((++iter & 15u) == 0) {
+            if (lane == 0 && (iter & 1023u) == 0) atomicAdd(a.progress, 1ull);
+            if (ld_volatile(a.error)) break;
+            if (donate) {
+                uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
+                if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) {
+                    try_donate(a, frames, fdepth, wc, qh - qt);
+                    const uint32_t hi2 = nq + frames[fdepth].end;  // lowered when level 0 was split
+                    const uint32_t keep = hi2 >= 32 ? ~0u : ((1u << hi2) - 1u);
+                    if (depth == 0)
+                        pend &= keep;
+                    else if (lane == 0)
+                        st[0].pend &= keep;
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    if (lane == 0) frames[fdepth].next = frames[fdepth].end;
+    __syncwarp();
+}
+
 #ifdef MBE_PROFILE
 // Spreads one idle interval [w0, w1) over the 4 ms bins of the kernel-time
 // histogram (idle ns per bin, then waits ending per bin).
@@ -1401,10 +1589,17 @@ __device__ void prof_idle(const EngineArgs& a, unsigned long long t0, unsigned l
 }
 #endif
 
-__global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
+#ifndef MBE_DFS_MIN_BLOCKS
+#define MBE_DFS_MIN_BLOCKS 2  // 16 warps per SM with a 128-register budget: no spills
+#endif
+__global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(EngineArgs a) {
     __shared__ uint32_t sLi[kWarpsB][kSmemW];
     __shared__ uint32_t sNz[kWarpsB][kSmemW];
-    __shared__ uint32_t sBucket[kWarpsB][32];
+    __shared__ uint32_t sBucket[kWarpsB][64];
+    __shared__ uint32_t sRow[kWarpsB][kShRows];
+    __shared__ uint32_t sPos[kWarpsB][kShRows];
+    __shared__ unsigned long long sKeys[kWarpsB][kShRows];
+    __shared__ SolveLevel sSolve[kWarpsB][kSolveRows + 1];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const size_t gw = (size_t)blockIdx.x * kWarpsB + warp;
     Frame* frames = a.frames + gw * a.max_frames;
@@ -1423,6 +1618,10 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
     wc.sBucket = sBucket[warp];
+    wc.shRow = sRow[warp];
+    wc.shPos = sPos[warp];
+    wc.shKeys = sKeys[warp];
+    wc.solve = sSolve[warp];
     wc.slab_off = wc.slab_end = 0;
 #ifdef MBE_PROFILE
     __shared__ unsigned long long sTab[kProfTB * kProfTC * 2];
@@ -1538,6 +1737,12 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
                     if (f.next >= f.end) continue;
                 }
                 const uint32_t* nd = (const uint32_t*)f.node;
+                if (prefilter && (((const NodeHdr*)nd)->flags & kRecPacked) && ((const NodeHdr*)nd)->n <= a.solve_rows) {
+                    PROF_T0();
+                    solve_small(a, G, nd, frames, depth, wc, acc, donate);
+                    PROF_ADD(wc.prof, kProfSolve);
+                    continue;
+                }
                 if (prefilter && ((const NodeHdr*)nd)->W == 1) {
                     PROF_T0();
                     const RecView R = rec_view(nd);
@@ -1548,6 +1753,7 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
                     uint32_t mask = prefilter_w1(R, f.next, nb, acc);
 #ifdef MBE_PROFILE
                     PROF_TAB(9, c0p, clock64() - c0p);
+            if ((R.flags & kRecPacked) && R.n <= 32) PROF_VAL(wc.prof, kProfSmallPre, clock64() - c0p);
 #endif
                     PROF_ADD(wc.prof, kProfPrefilter);
                     evals += nb;
@@ -1578,6 +1784,10 @@ __global__ void __launch_bounds__(kThreadsB, 3) dfs_kernel(EngineArgs a) {
             ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, wc, acc, false, known_max);
 #ifdef MBE_PROFILE
             PROF_TAB(min(7, 31 - __clz(pW)), c0e, clock64() - c0e);
+            if ((((const NodeHdr*)f.node)->flags & kRecPacked) && ((const NodeHdr*)f.node)->n <= 32)
+                PROF_VAL(wc.prof, kProfSmallEval, clock64() - c0e);
+            else if (co.rec && (((const NodeHdr*)co.rec)->flags & kRecPacked) && ((const NodeHdr*)co.rec)->n <= 32)
+                PROF_VAL(wc.prof, kProfSmallBuild, clock64() - c0e);
             PROF_TAB(10, 0, depth);
 #endif
             evals++;
@@ -1758,6 +1968,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.minR = cfg.minR;
     a.donate_min = std::max(2u, cfg.donate_min);
     a.donate_copy = 1;
+    a.solve_rows = kSolveRows;
+    if (const char* e = std::getenv("MBE_SOLVE_ROWS")) a.solve_rows = std::min<uint32_t>((uint32_t)std::atoi(e), kSolveRows);
     if (const char* e = std::getenv("MBE_DONATE_COPY")) a.donate_copy = (uint32_t)std::atoi(e);
     a.root_next = &ctrl->root_next;
     a.retry = (uint32_t*)eb.retry_in.ptr;
@@ -1864,7 +2076,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
                 while (kc < scr_n) kc <<= 1;
-                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 5 * kc, 32);
+                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 2 * kc, 32);
                 if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
                 a.scratch = (uint32_t*)eb.scratch.ptr;
                 a.scratch_words = (uint32_t)sw;
@@ -1944,12 +2156,15 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     {
         unsigned long long hp[kProfSlots];
         MBE_CUDA_TRY(cudaMemcpy(hp, a.prof, sizeof hp, cudaMemcpyDeviceToHost));
-        static const char* names[] = {"pop", "replay", "donate", "prefilter", "qscan", "expand", "build"};
+        static const char* names[] = {"pop", "replay", "donate", "prefilter", "qscan", "expand", "build", "solve",
+                                      "b.gather", "b.sort", "b.reduce", "b.write", "sum xi", "sum m", "sum nq2", "sum npp",
+                                      "small eval", "small pre", "small bld"};
         unsigned long long tot = 0;
-        for (int q = 0; q < kProfSections; q++) tot += hp[2 * q];
+        for (int q = 0; q < kProfMain; q++) tot += hp[2 * q];
         for (int q = 0; q < kProfSections; q++)
-            std::fprintf(stderr, "prof %-10s cycles %14llu (%5.1f%%) events %12llu\n", names[q], hp[2 * q],
-                         tot ? 100.0 * hp[2 * q] / tot : 0.0, hp[2 * q + 1]);
+            std::fprintf(stderr, "prof %-10s cycles %14llu (%5.1f%%) events %12llu avg %.1f\n", names[q], hp[2 * q],
+                         tot ? 100.0 * hp[2 * q] / tot : 0.0, hp[2 * q + 1],
+                         hp[2 * q + 1] ? (double)hp[2 * q] / hp[2 * q + 1] : 0.0);
         std::vector<unsigned long long> ex(nwarpsB);
         MBE_CUDA_TRY(cudaMemcpy(ex.data(), a.prof + kProfSlots, sizeof(unsigned long long) * nwarpsB,
                                 cudaMemcpyDeviceToHost));

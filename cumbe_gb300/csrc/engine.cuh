@@ -66,6 +66,19 @@ enum : int {
     kProfQscan,          // L_i + maximality scan of single evaluations
     kProfExpand,         // expansion (P scan) + hash of maximal children
     kProfBuild,          // child record construction
+    kProfSolve,          // register-resident enumeration of small packed records
+    kProfMain,           // sections above partition the warp time; below: detail of packed builds
+    kProfBGather = kProfMain,  // Q' gather
+    kProfBSort,          // Q' bucket sort and permutation
+    kProfBReduce,        // Q' reduction
+    kProfBWrite,         // P' sort, record write
+    kProfSumXi,          // value sums (cycles field) per packed build (events field)
+    kProfSumM,
+    kProfSumNq2,
+    kProfSumNpp,
+    kProfSmallEval,      // evaluations (cycles) of children of packed records with <= 32 rows
+    kProfSmallPre,       // prefilter batches (cycles) on such records
+    kProfSmallBuild,     // builds of packed records with <= 32 rows (cycles)
     kProfSections,
     kProfSlots = 2 * kProfSections,
     kProfBins = 512,           // idle-time histogram over kernel time
@@ -124,6 +137,7 @@ struct EngineArgs {
     uint32_t minL, minR;       // thresholds in L/R orientation (batched: same for all)
     uint32_t donate_min;
     uint32_t donate_copy;      // 1: donate small arena records by copy into the pool
+    uint32_t solve_rows;       // packed records with at most this many rows (<= 32) are solved in registers
     // root list: (graph, rank) pairs, processed from index 0
     const uint2* roots;
     uint32_t n_roots;
