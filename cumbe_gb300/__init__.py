@@ -257,12 +257,36 @@ class Engine:
         _check(lib().mbe_graph_release(self._h, g.handle), "mbe_graph_release")
 
     def enumerate(self, g: Graph, variant: str = "cuMBE", min_rows: int = 0, min_cols: int = 0,
-                  hash: bool = True, **tuning) -> Result:
-        o = _opts(flags=OPT_TIMING | (0 if hash else OPT_NO_HASH), min_rows=min_rows, min_cols=min_cols, **tuning)
+                  hash: bool = True, emit_cap: int = 0, emit_ids_cap: int = 0, **tuning) -> Result:
+        """Counts (and hashes) the maximal bicliques of g.  emit_cap > 0 also
+        returns them (MBE_OPT_EMIT) as Result.bicliques, a list of (rows,
+        cols) tuples in file ids, with room for emit_cap bicliques and
+        emit_ids_cap ids (default 64 per biclique); a run whose output does
+        not fit raises, naming how many were written."""
+        flags = OPT_TIMING | (0 if hash else OPT_NO_HASH) | (OPT_EMIT if emit_cap else 0)
+        o = _opts(flags=flags, min_rows=min_rows, min_cols=min_cols, **tuning)
+        if emit_cap:
+            ids_cap = emit_ids_cap or 64 * emit_cap
+            offs = np.zeros(emit_cap + 1, dtype=np.uint32)
+            nrows = np.zeros(emit_cap, dtype=np.uint32)
+            ids = np.zeros(max(1, ids_cap), dtype=np.uint32)
+            o.emit_offsets = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+            o.emit_nrows = nrows.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+            o.emit_ids = ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+            o.emit_cap_bicliques = emit_cap
+            o.emit_cap_ids = ids_cap
         r = _Result()
         _check(lib().mbe_enumerate(self._h, g.handle, VARIANTS[variant], ctypes.byref(o), ctypes.byref(r)),
                "mbe_enumerate")
-        return Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep)
+        out = Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep)
+        if emit_cap:
+            bl = []
+            for k in range(r.emitted):
+                a, b = int(offs[k]), int(offs[k + 1])
+                nr = int(nrows[k])
+                bl.append((tuple(int(v) for v in ids[a:a + nr]), tuple(int(v) for v in ids[a + nr:b])))
+            out.bicliques = bl
+        return out
 
     def batch(self, graphs: list[Graph], variant: str = "cuMBE", min_rows: int = 0, min_cols: int = 0,
               **tuning) -> tuple[list[Result], float]:

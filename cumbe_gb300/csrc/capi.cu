@@ -132,7 +132,8 @@ namespace mbe {
 // file orientation, so a list mixing orientations with thresholds runs
 // once per orientation group.
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
-                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats) {
+                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
+                    const EmitTarget* emit) {
     const uint32_t n = (uint32_t)devs.size();
     bool any_swapped = false, any_plain = false;
     for (const DeviceGraph* d : devs) (d->swapped ? any_swapped : any_plain) = true;
@@ -158,6 +159,7 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
             for (const uint2& r : roots)
                 if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
         EngineConfig cfg = make_config(variant, opts, sw);
+        cfg.emit = emit;
         std::vector<ResultAcc> part;
         EngineStats ps;
         mbe_status st = engine_run(eb, s, cfg, devs, split ? sel : roots, part, &ps, io);
@@ -181,10 +183,71 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
 
 }  // namespace mbe
 
+// Output stream of one enumeration: device buffers sized by the caller's
+// capacities, then compacted into the caller's host buffers in
+// reservation order (offsets[k]..offsets[k+1] = rows then cols of
+// biclique k).
+struct EmitRun {
+    EmitTarget t;
+    mbe_status setup(mbe_ctx* ctx, const mbe_opts* o) {
+        if (!o->emit_offsets || !o->emit_ids || !o->emit_nrows || !o->emit_cap_bicliques)
+            return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT needs emit_offsets, emit_ids, emit_nrows and capacities");
+        if (o->emit_cap_ids >= (1ull << 32))
+            return fail(MBE_ERR_INVALID_ARG, "emit_cap_ids must be below 2^32 (offsets are 32-bit)");
+        EngineBuffers& eb = ctx->eb;
+        mbe_status st;
+        const size_t capb = (size_t)o->emit_cap_bicliques, capi = std::max<size_t>(1, (size_t)o->emit_cap_ids);
+        if ((st = eb.e_ids.ensure(4 * capi)) || (st = eb.e_start.ensure(8 * capb)) ||
+            (st = eb.e_nrows.ensure(4 * capb)) || (st = eb.e_ncols.ensure(4 * capb)) ||
+            (st = eb.e_ctl.ensure(3 * sizeof(unsigned long long))))
+            return st;
+        t.ids = (uint32_t*)eb.e_ids.ptr;
+        t.cap_ids = o->emit_cap_ids;
+        t.start = (unsigned long long*)eb.e_start.ptr;
+        t.nrows = (uint32_t*)eb.e_nrows.ptr;
+        t.ncols = (uint32_t*)eb.e_ncols.ptr;
+        t.cap_b = o->emit_cap_bicliques;
+        t.ctl = (unsigned long long*)eb.e_ctl.ptr;
+        return MBE_OK;
+    }
+    // Copies the stream to the caller's buffers; *emitted = bicliques
+    // written; MBE_ERR_CAPACITY when some did not fit.
+    mbe_status finish(mbe_ctx* ctx, const mbe_opts* o, uint64_t* emitted) {
+        unsigned long long ctl[3];
+        mbe_status st = check_cuda(cudaMemcpy(ctl, t.ctl, sizeof ctl, cudaMemcpyDeviceToHost), "emit readback");
+        if (st) return st;
+        const size_t K = (size_t)std::min<unsigned long long>(ctl[1], t.cap_b);
+        const size_t used = (size_t)std::min<unsigned long long>(ctl[0], t.cap_ids);
+        std::vector<unsigned long long> start(K);
+        std::vector<uint32_t> nr(K), nc(K), ids(used);
+        if (K && ((st = check_cuda(cudaMemcpy(start.data(), t.start, 8 * K, cudaMemcpyDeviceToHost), "emit")) ||
+                  (st = check_cuda(cudaMemcpy(nr.data(), t.nrows, 4 * K, cudaMemcpyDeviceToHost), "emit")) ||
+                  (st = check_cuda(cudaMemcpy(nc.data(), t.ncols, 4 * K, cudaMemcpyDeviceToHost), "emit"))))
+            return st;
+        if (used && (st = check_cuda(cudaMemcpy(ids.data(), t.ids, 4 * used, cudaMemcpyDeviceToHost), "emit")))
+            return st;
+        ctx->io.d2h += sizeof ctl + 16 * K + 4 * used;
+        uint64_t off = 0;
+        for (size_t k = 0; k < K; k++) {
+            const uint32_t sz = nr[k] + nc[k];
+            o->emit_offsets[k] = (uint32_t)off;
+            o->emit_nrows[k] = nr[k];
+            std::memcpy(o->emit_ids + off, ids.data() + start[k], 4ull * sz);
+            off += sz;
+        }
+        o->emit_offsets[K] = (uint32_t)off;
+        *emitted = K;
+        if (ctl[2])
+            return fail(MBE_ERR_CAPACITY, "emit buffers full: " + std::to_string(K) +
+                                              " bicliques written (count and hash cover all)");
+        return MBE_OK;
+    }
+};
+
 static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
                              const mbe_opts* opts, mbe_result* out, float* total_ms) {
-    if (opts && (opts->flags & MBE_OPT_EMIT))
-        return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT is not supported by this build");
+    const bool emit = opts && (opts->flags & MBE_OPT_EMIT);
+    if (emit && n != 1) return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT takes one graph (mbe_enumerate)");
     mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (st) return st;
     std::vector<const DeviceGraph*> devs(n);
@@ -192,9 +255,12 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         if (!graphs[i]) return fail(MBE_ERR_INVALID_ARG, "null graph");
         if ((st = ensure_resident(ctx, graphs[i], &devs[i]))) return st;
     }
+    EmitRun er;
+    if (emit && (st = er.setup(ctx, opts))) return st;
     std::vector<ResultAcc> acc;
     EngineStats stats;
-    if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, devs, variant, opts, acc, stats))) return st;
+    if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, devs, variant, opts, acc, stats, emit ? &er.t : nullptr)))
+        return st;
     ctx->last_stats = stats;
     for (uint32_t i = 0; i < n; i++) {
         mbe_result& r = out[i];
@@ -208,6 +274,7 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
         r.ms_prep = stats.ms_expand;
     }
     if (total_ms) *total_ms = stats.ms_expand + stats.ms_dfs;
+    if (emit) return er.finish(ctx, opts, &out[0].emitted);
     return MBE_OK;
 }
 

@@ -55,7 +55,7 @@ constexpr uint32_t kSolveRows = 32;      // packed records with at most this man
 // One saved level of the register-resident small-record search (row masks
 // over the record's rows, one row per lane).
 struct SolveLevel {
-    uint32_t L, Q, P, pend, nR, pad;
+    uint32_t L, Q, P, pend, nR, Rm;  // Rm: rows added to R below the record (output stream)
     unsigned long long sR;
 };
 constexpr uint32_t kDonateSlabMax = 8192;      // arena records up to this size are copied into a slab
@@ -205,10 +205,75 @@ __device__ __forceinline__ uint32_t next_pow2(uint32_t x) {
 }
 
 // ---------------------------------------------------------------------------
+// Output stream (MBE_OPT_EMIT).  A counted biclique reserves room for its
+// file rows then its file cols (ids in no particular order within a side);
+// a biclique that does not fit is dropped and the overflow flag set, while
+// the count and hash still cover it.  R members are ranks on the device and
+// leave as file ids through r_orig; L members are file ids already.
+
+// Reserves room for a biclique with nr R members and nl L members; returns
+// the id offset, or ~0 when the buffers are full.  Warp-collective.
+__device__ __noinline__ unsigned long long emit_reserve(const EngineArgs& a, uint32_t nr, uint32_t nl,
+                                                        uint32_t swapped) {
+    unsigned long long o = ~0ull;
+    if (lane_id() == 0) {
+        const uint32_t na = swapped ? nl : nr, nb = swapped ? nr : nl;
+        const unsigned long long sz = (unsigned long long)na + nb;
+        const unsigned long long oo = atomicAdd(&a.emit_ctl[0], sz);
+        unsigned long long k = ~0ull;
+        if (oo + sz <= a.emit_cap_ids) k = atomicAdd(&a.emit_ctl[1], 1ull);
+        if (k < a.emit_cap_b) {
+            a.emit_start[k] = oo;
+            a.emit_nrows[k] = na;
+            a.emit_ncols[k] = nb;
+            o = oo;
+        } else {
+            atomicExch(&a.emit_ctl[2], 1ull);
+        }
+    }
+    return __shfl_sync(kFull, o, 0);
+}
+
+// Copies the R list of record nd (ranks) to dst, as file ids when r_orig is
+// given.  Warp-collective.
+__device__ __forceinline__ void copy_rlist(const uint32_t* nd, uint32_t* dst, const uint32_t* r_orig) {
+    const NodeHdr* h = (const NodeHdr*)nd;
+    const uint32_t* rl = nd + h->rlist;
+    for (uint32_t t = lane_id(); t < h->nRset; t += 32) dst[t] = r_orig ? r_orig[rl[t]] : rl[t];
+}
+
+// R list of the child record of x_i (ranks): the parent's list, x_i, the
+// absorbed.  Warp-collective.
+__device__ __noinline__ void write_child_rlist(const uint32_t* nd, uint32_t xcand, const uint32_t* abs,
+                                               uint32_t nabs, uint32_t* dst) {
+    const uint32_t nrec = ((const NodeHdr*)nd)->nRset;
+    copy_rlist(nd, dst, nullptr);
+    if (lane_id() == 0) dst[nrec] = xcand;
+    for (uint32_t t = lane_id(); t < nabs; t += 32) dst[nrec + 1 + t] = abs[t];
+}
+
+// x and the candidates of root x absorbed into R (count d = |N(x)|), as
+// ranks, or as file ids when r_orig is given.  Warp-collective.
+__device__ void root_rlist(uint32_t x, const uint32_t* cl, const uint32_t* cntA, uint32_t n, uint32_t d,
+                           uint32_t* dst, const uint32_t* r_orig) {
+    const unsigned lane = lane_id();
+    if (lane == 0) dst[0] = r_orig ? r_orig[x] : x;
+    uint32_t m = 1;
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t i = base + lane;
+        const uint32_t v = i < n ? cl[i] : 0u;
+        const bool ab = i < n && v > x && cntA[i] == d;
+        const unsigned b = __ballot_sync(kFull, ab);
+        if (ab) dst[m + __popc(b & lanemask_lt())] = r_orig ? r_orig[v] : v;
+        m += __popc(b);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Phase A: root expansion
 
 __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
-    __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax;
+    __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax, s_counted;
     __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
     __shared__ unsigned long long s_sabs, s_sl, s_rec, s_scan;
     __shared__ unsigned long long s_keys[2048];
@@ -235,7 +300,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                     s_idx = i;
             }
             s_ncand = 0;
-            s_nq = s_np = s_nabs = s_nonmax = 0;
+            s_nq = s_np = s_nabs = s_nonmax = s_counted = 0;
             s_sabs = s_sl = s_scan = 0;
         }
         __syncthreads();
@@ -344,7 +409,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
         const uint32_t nRset = 1 + s_nabs;
         const uint32_t n2 = s_nq + s_np;
         const bool emit_task = !s_nonmax && s_np > 0 && nRset + s_np >= a.minR;
-        const uint64_t rw = record_words(W, n2);
+        const uint64_t rw = a.emit ? record_words_r(W, n2, false, nRset) : record_words(W, n2);
         if (threadIdx.x == 0) {
             s_rec = ~0ull;
             bool ok = true;
@@ -370,10 +435,21 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                     unsigned long long sR = G.eR[x] + s_sabs;
                     atomicAdd(&r->count, 1ull);
                     atomicAdd(&r->hash, (unsigned long long)side_hash(G, s_sl, d, sR, nRset));
+                    s_counted = 1;
                 }
             }
         }
         __syncthreads();
+        if (a.emit && s_counted && warp == 0) {
+            // the root biclique: R = x + the absorbed, L = N(x)
+            const unsigned long long o = emit_reserve(a, nRset, d, G.swapped);
+            if (o != ~0ull) {
+                uint32_t* dr = a.emit_ids + o + (G.swapped ? d : 0);
+                uint32_t* dl = a.emit_ids + o + (G.swapped ? 0 : nRset);
+                root_rlist(x, cl, cntA, n, d, dr, G.r_orig);
+                for (uint32_t t = lane; t < d; t += 32) dl[t] = L0[t];
+            }
+        }
         if (emit_task && s_rec != ~0ull) {
             // 4. order: Q part by rank, then P part by (count, rank)
             uint32_t N = next_pow2(max(n, 2u));
@@ -553,6 +629,17 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                         h->words = (uint32_t)record_words(W, n3);
                     }
                 }
+                if (a.emit) {
+                    // R list after the (compacted) rows: x + the absorbed, as ranks
+                    const uint32_t nfin = nq2 < s_nq ? nq2 + s_np : n2;
+                    const uint32_t rl = (uint32_t)record_words(W, nfin);
+                    __syncthreads();
+                    if (warp == 0) root_rlist(x, cl, cntA, n, d, rec + rl, nullptr);
+                    if (threadIdx.x == 0) {
+                        ((NodeHdr*)rec)->rlist = rl;
+                        ((NodeHdr*)rec)->words = rl + pad4(nRset);
+                    }
+                }
                 __threadfence();
                 __syncthreads();
                 if (threadIdx.x == 0) {
@@ -585,6 +672,7 @@ struct WarpCtx {
     uint32_t* sLi;
     uint32_t* sNz;
     uint32_t* scrPack;     // 2 x kc words: srow, spos of a packed build too large for shared memory
+    uint32_t* scrAbs;      // scr_n words: ranks absorbed by the child being evaluated (output stream only)
     uint32_t* sBucket;     // 64 words of shared memory: Q' then P' count buckets
     uint32_t* shRow;       // kShRows Q' rows of a packed build (shared memory)
     uint32_t* shPos;       // their parent positions
@@ -696,6 +784,59 @@ __device__ __forceinline__ RecView rec_view(const uint32_t* nd) {
     v.cnt = v.cand + pad4(v.n);
     v.M = v.cnt + pad4(v.n);
     return v;
+}
+
+// Writes the L members of L_i (words Li[0..nnz) at record words Nz[]) of
+// record R (root nd) to dst in bit order.  Warp-collective.
+__device__ __forceinline__ void write_lset(const GraphView& G, const uint32_t* nd, const RecView& R,
+                                           const uint32_t* Li, const uint32_t* Nz, uint32_t nnz, uint32_t* dst) {
+    const unsigned lane = lane_id();
+    if (R.flags & kRecPacked) {  // packed maps hold L vertices
+        const uint32_t bits = Li[0];
+        if ((bits >> lane) & 1u) dst[__popc(bits & lanemask_lt())] = R.map[lane];
+        return;
+    }
+    const uint32_t* L0 = G.r_adj + G.r_ptr[((const NodeHdr*)nd)->root];
+    uint32_t before = 0;
+    for (uint32_t k = 0; k < nnz; k++) {
+        const uint32_t w = Li[k];
+        if ((w >> lane) & 1u) dst[before + __popc(w & lanemask_lt())] = L0[R.map[Nz[k]] * 32 + lane];
+        before += __popc(w);
+    }
+}
+
+// Child x_i of record nd is a counted maximal biclique: R = the record's R
+// list + x_i + the absorbed ranks abs[0..nabs), L = L_i.  Warp-collective.
+__device__ __noinline__ void emit_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t xi,
+                                        const uint32_t* Li, const uint32_t* Nz, uint32_t nnz, uint32_t li,
+                                        const uint32_t* abs, uint32_t nabs) {
+    const RecView R = rec_view(nd);
+    const uint32_t nrec = ((const NodeHdr*)nd)->nRset, nr = nrec + 1 + nabs;
+    const unsigned long long o = emit_reserve(a, nr, li, G.swapped);
+    if (o == ~0ull) return;
+    uint32_t* dr = a.emit_ids + o + (G.swapped ? li : 0);
+    uint32_t* dl = a.emit_ids + o + (G.swapped ? 0 : nr);
+    copy_rlist(nd, dr, G.r_orig);
+    if (lane_id() == 0) dr[nrec] = G.r_orig[R.cand[xi]];
+    for (uint32_t t = lane_id(); t < nabs; t += 32) dr[nrec + 1 + t] = G.r_orig[abs[t]];
+    write_lset(G, nd, R, Li, Nz, nnz, dl);
+}
+
+// A counted biclique of the register-resident search below packed record
+// nd: R = the record's R list + the candidates of rows in Rm, L = the bits
+// of L2 (over the record's L bits).  Warp-collective.
+__device__ __noinline__ void emit_solved(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t Rm,
+                                         uint32_t L2) {
+    const unsigned lane = lane_id();
+    const RecView R = rec_view(nd);
+    const uint32_t nrec = ((const NodeHdr*)nd)->nRset, nr = nrec + __popc(Rm), nl = __popc(L2);
+    const unsigned long long o = emit_reserve(a, nr, nl, G.swapped);
+    if (o == ~0ull) return;
+    uint32_t* dr = a.emit_ids + o + (G.swapped ? nl : 0);
+    uint32_t* dl = a.emit_ids + o + (G.swapped ? 0 : nr);
+    copy_rlist(nd, dr, G.r_orig);
+    if ((Rm >> lane) & 1u) dr[nrec + __popc(Rm & lanemask_lt())] = G.r_orig[R.cand[lane]];
+    if ((L2 >> lane) & 1u) dl[__popc(L2 & lanemask_lt())] = R.map[lane];
 }
 
 // bits of x selected by m, packed to the low end in order
@@ -903,7 +1044,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     bucket_offsets(sbp);
     // allocate and write
     const uint32_t n2 = nq2 + npp;
-    const uint64_t rw = record_words(1, n2, true);
+    const uint64_t rw = a.emit ? record_words_r(1, n2, true, nR2) : record_words(1, n2, true);
     uint32_t* rec;
     if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
         rec = wc.arena + wc.arena_top;
@@ -936,10 +1077,13 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
         h2->depth = h->depth + 1;
         h2->sR = sR2;
         h2->words = (uint32_t)rw;
-        h2->rlist = 0;
+        h2->rlist = a.emit ? (uint32_t)record_words(1, n2, true) : 0u;
         h2->flags = kRecPacked;
         Lm2[0] = li == 32 ? 0xFFFFFFFFu : ((1u << li) - 1u);
     }
+    if (a.emit)
+        write_child_rlist((const uint32_t*)h, R.cand[xi], wc.scrAbs, nR2 - h->nRset - 1,
+                          rec + record_words(1, n2, true));
     // lane t < li: L vertex of the t-th set bit of L_i (words in order)
     if (lane < li) {
         uint32_t vtx;
@@ -1090,7 +1234,7 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
 
     // 5d. allocate and write the record
     const uint32_t n2 = nq2 + npp, W2 = nnz;  // |L_i| > 32 here: an unpacked child
-    const uint64_t rw = record_words(W2, n2, false);
+    const uint64_t rw = a.emit ? record_words_r(W2, n2, false, nR2) : record_words(W2, n2, false);
     uint32_t* rec;
     if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
         rec = wc.arena + wc.arena_top;
@@ -1123,9 +1267,11 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
         h2->depth = h->depth + 1;
         h2->sR = sR2;
         h2->words = (uint32_t)rw;
-        h2->rlist = 0;
+        h2->rlist = a.emit ? (uint32_t)record_words(W2, n2, false) : 0u;
         h2->flags = 0u;
     }
+    if (a.emit)
+        write_child_rlist(nd, cand[xi], wc.scrAbs, nR2 - h->nRset - 1, rec + record_words(W2, n2, false));
     for (uint32_t k = lane; k < W2; k += 32) {
         map2[k] = R.map[Nz[k]];
         Lm2[k] = Li[k];
@@ -1258,6 +1404,7 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
             if (absorbed) sabs += G.eR[cand[c]];
             unsigned pb = __ballot_sync(kFull, partial), ab = __ballot_sync(kFull, absorbed);
             if (partial) keysP[npp + __popc(pb & lanemask_lt())] = ((unsigned long long)cc << 32) | (c - nq);
+            if (a.emit && absorbed) wc.scrAbs[nabs + __popc(ab & lanemask_lt())] = cand[c];
             if (packed_child && pb) {
                 unsigned grp = __match_any_sync(kFull, partial ? cc : 32u);
                 if (partial && (grp & lanemask_lt()) == 0) atomicAdd(&wc.sBucket[32 + cc], (uint32_t)__popc(grp));
@@ -1291,6 +1438,7 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
         sl = warp_sum(sl);
         acc.count++;
         acc.hash += side_hash(G, sl, li, sR2, nR2);
+        if (a.emit && !replay) emit_child(a, G, nd, xi, Li, Nz, nnz, li, wc.scrAbs, nabs);
     }
 
     // 5. child record
@@ -1495,7 +1643,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
     const uint32_t Qroot = (1u << nq) - 1u;  // nq < n <= 32
     const uint32_t lo = nq + frames[fdepth].next, hi = nq + frames[fdepth].end;
     const uint32_t kids0 = (hi >= 32 ? ~0u : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-    uint32_t L = Lroot, Q = Qroot, P = all & ~Qroot, nR = h->nRset;
+    uint32_t L = Lroot, Q = Qroot, P = all & ~Qroot, nR = h->nRset, Rm = 0;
     unsigned long long sR = h->sR;
     uint32_t pend = solve_maximal(row, L, Q, P, kids0);
     acc.nodes += __popc(kids0);
@@ -1512,6 +1660,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
             P = sv.P;
             pend = sv.pend;
             nR = sv.nR;
+            Rm = sv.Rm;
             sR = sv.sR;
             continue;
         }
@@ -1536,14 +1685,16 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
             const unsigned long long sl = warp_sum(((L2 >> lane) & 1u) ? eL : 0ull);
             acc.count++;
             acc.hash += side_hash(G, sl, l2, sR2, nR2);
+            if (a.emit) emit_solved(a, G, nd, Rm | (1u << x) | absorbed, L2);
         }
         if (P2 && l2 >= a.minL && nR2 + __popc(P2) >= a.minR) {
             const uint32_t pend2 = solve_maximal(row, L2, Q2, P2, P2);
             acc.nodes += __popc(P2);
             if (pend2) {
-                if (lane == 0) st[depth] = SolveLevel{L, Q, P, pend, nR, 0u, sR};
+                if (lane == 0) st[depth] = SolveLevel{L, Q, P, pend, nR, Rm, sR};
                 __syncwarp();
                 depth++;
+                Rm |= (1u << x) | absorbed;
                 L = L2;
                 Q = Q2;
                 P = P2;
@@ -1615,6 +1766,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
     wc.scrKeysP = (unsigned long long*)(scr + koff);
     wc.scrKeysQ = wc.scrKeysP + a.scr_kc;
     wc.scrPack = (uint32_t*)(wc.scrKeysQ + a.scr_kc);
+    wc.scrAbs = wc.scrPack + 2 * (size_t)a.scr_kc;
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
     wc.sBucket = sBucket[warp];
@@ -1848,7 +2000,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 void EngineBuffers::release() {
     for (DevBuf* b : {&graphs, &roots, &ctrl, &tasks, &ready, &cmap, &a_cl, &a_cnt, &a_keys, &pool, &arena, &frames,
-                      &scratch, &results, &retry_in, &retry_list})
+                      &scratch, &results, &retry_in, &retry_list, &e_ids, &e_start, &e_nrows, &e_ncols, &e_ctl})
         b->free();
 }
 
@@ -2001,6 +2153,16 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.error = &ctrl->error;
     a.error_info = &ctrl->error_info;
     a.timeout_ns = cfg.timeout_ns;
+    if (cfg.emit) {
+        a.emit = 1;
+        a.emit_ids = cfg.emit->ids;
+        a.emit_cap_ids = cfg.emit->cap_ids;
+        a.emit_start = cfg.emit->start;
+        a.emit_nrows = cfg.emit->nrows;
+        a.emit_ncols = cfg.emit->ncols;
+        a.emit_cap_b = cfg.emit->cap_b;
+        a.emit_ctl = cfg.emit->ctl;
+    }
 #ifdef MBE_PROFILE
     static unsigned long long* prof_dev = nullptr;
     static size_t prof_n = 0;
@@ -2034,6 +2196,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         a.pool_watermark = pool_words / 2;
         MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));  // kernels restore -1 after each root
         MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
+        if (cfg.emit) MBE_CUDA_TRY(cudaMemsetAsync(cfg.emit->ctl, 0, 3 * sizeof(unsigned long long), s));
         ms_a = ms_b = 0;
         chunks = 0;
         result = MBE_OK;
@@ -2076,7 +2239,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
                 while (kc < scr_n) kc <<= 1;
-                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 2 * kc, 32);
+                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 2 * kc +
+                                         (cfg.emit ? scr_n : 0), 32);
                 if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
                 a.scratch = (uint32_t*)eb.scratch.ptr;
                 a.scratch_words = (uint32_t)sw;

@@ -95,6 +95,12 @@ __host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n, bool pa
     return kHdrWords + (packed ? 32ull : pad4(W)) + pad4(W) + 2ull * pad4(n) + (((uint64_t)W * n + 3) & ~3ull);
 }
 
+// Words of a record that also carries its R list (nr ranks; output stream
+// only), stored right after the bit rows at word offset record_words().
+__host__ __device__ inline uint64_t record_words_r(uint32_t W, uint32_t n, bool packed, uint32_t nr) {
+    return record_words(W, n, packed) + pad4(nr);
+}
+
 // A unit of work: children [begin, end) of the node reached from the pool
 // record `node` by following child indices path[0..plen).  The receiver
 // re-derives the nodes on the path (deterministic), so donating a node that
@@ -181,6 +187,16 @@ struct EngineArgs {
     // section cycle counters (builds with -DMBE_PROFILE only; else null)
     unsigned long long* prof;  // [kProfSlots + warps + 2 * kProfBins]
     uint32_t prof_warps;
+    // output stream (MBE_OPT_EMIT; emit == 0 otherwise): each counted
+    // biclique reserves room for its file rows then its file cols
+    uint32_t emit;
+    uint32_t* emit_ids;                 // [emit_cap_ids]
+    unsigned long long emit_cap_ids;
+    unsigned long long* emit_start;     // [emit_cap_b] id offset of each biclique
+    uint32_t* emit_nrows;               // [emit_cap_b] |A| (file rows)
+    uint32_t* emit_ncols;               // [emit_cap_b] |B| (file cols)
+    unsigned long long emit_cap_b;
+    unsigned long long* emit_ctl;       // [0] ids reserved, [1] bicliques reserved, [2] overflow
     // results
     ResultAcc* results;        // [n_graphs]
     int* error;

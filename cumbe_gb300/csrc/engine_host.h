@@ -21,10 +21,23 @@ struct DevBuf {
 struct EngineBuffers {
     DevBuf graphs, roots, ctrl, tasks, ready, cmap, a_cl, a_cnt, a_keys, pool, arena, frames, scratch, results,
         retry_in, retry_list;
+    DevBuf e_ids, e_start, e_nrows, e_ncols, e_ctl;  // output stream
     // sizes chosen at first use from the device's free memory
     uint32_t arena_words = 0;
     uint64_t pool_words = 0;
     void release();
+};
+
+// Device buffers of the output stream (MBE_OPT_EMIT), owned by the caller
+// of engine_run; emission is off when EngineConfig::emit is null.
+struct EmitTarget {
+    uint32_t* ids = nullptr;
+    unsigned long long cap_ids = 0;
+    unsigned long long* start = nullptr;
+    uint32_t* nrows = nullptr;
+    uint32_t* ncols = nullptr;
+    unsigned long long cap_b = 0;
+    unsigned long long* ctl = nullptr;  // 3 words, reset by engine_run at every attempt
 };
 
 struct EngineConfig {
@@ -37,6 +50,7 @@ struct EngineConfig {
     uint64_t pool_words = 0;            // node pool cap; 0 = engine default (grows on demand)
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
     unsigned long long timeout_ns = 60ull * 1000000000ull;
+    const EmitTarget* emit = nullptr;
 };
 
 struct EngineStats {
@@ -52,7 +66,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 
 // Enumeration of resident graphs with opts applied (capi.cu).
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
-                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats);
+                    mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
+                    const EmitTarget* emit = nullptr);
 
 // Raw launchers of the two enumeration kernels (256 threads per block;
 // dfs_kernel runs 8 warps per block).

@@ -5,10 +5,16 @@
 // added after the reference's: the canonical hash, bicliques/sec and the
 // device time split.  Exit status is non-zero on any error (the reference
 // ignores errors and prints a count of 0, src/main.cu:185-207).
+//
+// `--emit FILE` (no reference counterpart; the reference only counts) also
+// writes every maximal biclique to FILE, one per line: its rows, " | ",
+// its cols, each side in ascending file ids.  stdout is unchanged.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <vector>
 
 #include "mbe.h"
 
@@ -17,21 +23,72 @@ static int die(const char* what, mbe_status st) {
     return 1;
 }
 
+// Runs the enumeration again with the output stream on (buffers sized from
+// the count, the id buffer grown until it fits) and writes FILE.
+static int write_bicliques(mbe_ctx* ctx, const mbe_graph* g, mbe_variant var, uint64_t count, const char* path) {
+    std::vector<uint32_t> offs(count + 1), nrows(std::max<uint64_t>(count, 1));
+    uint64_t cap_ids = std::max<uint64_t>(1024, 16 * count);
+    std::vector<uint32_t> ids;
+    mbe_result res;
+    for (;;) {
+        ids.assign(cap_ids, 0);
+        mbe_opts o;
+        std::memset(&o, 0, sizeof o);
+        o.flags = MBE_OPT_EMIT;
+        o.emit_offsets = offs.data();
+        o.emit_nrows = nrows.data();
+        o.emit_ids = ids.data();
+        o.emit_cap_bicliques = std::max<uint64_t>(count, 1);
+        o.emit_cap_ids = cap_ids;
+        mbe_status st = mbe_enumerate(ctx, g, var, &o, &res);
+        if (st == MBE_OK) break;
+        if (st != MBE_ERR_CAPACITY || cap_ids >= 0xFFFFFFFFull) return die("emitting the bicliques", st);
+        cap_ids = std::min<uint64_t>(0xFFFFFFFFull, 2 * cap_ids);
+    }
+    FILE* f = std::fopen(path, "w");
+    if (!f) {
+        std::fprintf(stderr, "mbe: cannot write %s\n", path);
+        return 1;
+    }
+    std::vector<uint32_t> side;
+    for (uint64_t k = 0; k < res.emitted; k++) {
+        const uint32_t* p = ids.data() + offs[k];
+        const uint32_t nr = nrows[k], nc = offs[k + 1] - offs[k] - nr;
+        for (int s = 0; s < 2; s++) {
+            side.assign(p + (s ? nr : 0), p + (s ? nr + nc : nr));
+            std::sort(side.begin(), side.end());
+            for (size_t i = 0; i < side.size(); i++) std::fprintf(f, i ? " %u" : "%u", side[i]);
+            std::fputs(s ? "\n" : " | ", f);
+        }
+    }
+    std::fclose(f);
+    std::fprintf(stderr, "mbe: %llu bicliques written to %s\n", (unsigned long long)res.emitted, path);
+    return 0;
+}
+
 int main(int argc, char** argv) {
-    if (argc < 2) {
-        std::fprintf(stderr, "usage: %s <graph.bi> [cuMBE|noRS|noES|noWS]\n", argv[0]);
+    const char* emit_path = nullptr;
+    std::vector<const char*> pos;
+    for (int i = 1; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--emit") && i + 1 < argc)
+            emit_path = argv[++i];
+        else
+            pos.push_back(argv[i]);
+    }
+    if (pos.empty()) {
+        std::fprintf(stderr, "usage: %s <graph.bi> [cuMBE|noRS|noES|noWS] [--emit FILE]\n", argv[0]);
         return 2;
     }
     std::time_t now = std::time(nullptr);
-    std::string dataset = argv[1];
+    std::string dataset = pos[0];
     size_t slash = dataset.rfind('/');
     if (slash != std::string::npos) dataset = dataset.substr(slash + 1);
-    mbe_variant var = mbe_variant_from_name(argc > 2 ? argv[2] : "cuMBE");
+    mbe_variant var = mbe_variant_from_name(pos.size() > 1 ? pos[1] : "cuMBE");
     std::string algo = mbe_variant_name(var);
     std::string stem = dataset.substr(0, dataset.rfind('.'));
 
     mbe_graph* g = nullptr;
-    mbe_status st = mbe_graph_load_bi(argv[1], &g);
+    mbe_status st = mbe_graph_load_bi(pos[0], &g);
     if (st != MBE_OK) return die("loading the graph", st);
     mbe_graph_info info;
     mbe_graph_info_get(g, &info);
@@ -71,7 +128,8 @@ int main(int argc, char** argv) {
         std::fputs(tail, f);
         std::fclose(f);
     }
+    int rc = emit_path ? write_bicliques(ctx, g, var, res.count, emit_path) : 0;
     mbe_ctx_destroy(ctx);
     mbe_graph_free(g);
-    return 0;
+    return rc;
 }

@@ -117,7 +117,16 @@ typedef struct mbe_opts {
     uint32_t blocks_per_sm;
     uint32_t donate_min;         /* min remaining children to donate       */
     uint32_t stack_words;        /* per-warp DFS arena size, 32-bit words  */
-    /* optional output stream (MBE_OPT_EMIT): host buffers, see mbe_emit_* */
+    /* Optional output stream (MBE_OPT_EMIT; mbe_enumerate only).  The
+     * reference only counts (src/main.cu:207); this materialises each
+     * counted biclique k into the caller's host buffers:
+     *   emit_ids[emit_offsets[k] .. +emit_nrows[k]]     its rows (A),
+     *   emit_ids[.. emit_offsets[k+1]]                  its cols (B),
+     * in file ids, sides in no particular order, bicliques in no particular
+     * order; mbe_result.emitted = bicliques written.  When the capacities
+     * are too small the call returns MBE_ERR_CAPACITY with the result
+     * filled (count and hash still cover every biclique) and the buffers
+     * holding the first emitted ones.  emit_cap_ids must be < 2^32. */
     uint32_t* emit_offsets;      /* [emit_cap_bicliques+1] into emit_ids    */
     uint32_t* emit_ids;          /* rows of a biclique, then its cols       */
     uint32_t* emit_nrows;        /* [emit_cap_bicliques] |A| per biclique   */

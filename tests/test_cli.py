@@ -42,3 +42,28 @@ def test_cli_lines_and_result_file(built, tmp_path, variant):
     assert lines[7] == f"hash: {exp['hash']}"
     saved = (tmp_path / "result" / f"power_law_2k_1k_{algo}").read_text().splitlines()
     assert saved[1:6] == lines[1:6]
+
+
+@pytest.mark.gpu
+def test_cli_emit_file(built, tmp_path):
+    """`--emit FILE` writes every maximal biclique once: rows | cols, ascending
+    file ids; stdout keeps the reference's lines."""
+    exp = json.load(open(os.path.join(GOLD, "expected.json")))["power_law_2k_1k"]
+    path = os.path.join(GOLD, exp["file"])
+    out = tmp_path / "bicliques.txt"
+    r = subprocess.run([cm.CLI_PATH, path, "cuMBE", "--emit", str(out)], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines()[5] == f"maximal bicliques: {exp['count']}"
+    h, n = 0, 0
+    seen = set()
+    for line in out.read_text().splitlines():
+        a, b = line.split(" | ")
+        rows = [int(v) for v in a.split()]
+        cols = [int(v) for v in b.split()]
+        assert rows == sorted(rows) and cols == sorted(cols)
+        seen.add((tuple(rows), tuple(cols)))
+        h = (h + cm.biclique_hash(rows, cols)) & (2 ** 64 - 1)
+        n += 1
+    assert n == exp["count"] == len(seen)
+    assert f"0x{h:016x}" == exp["hash"]
