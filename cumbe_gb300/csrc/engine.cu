@@ -113,11 +113,22 @@ __device__ bool push_task(const EngineArgs& a, Task t) {
         }                                                                                                 \
     } while (0)
 #define PROF_T0() long long prof_t0__ = clock64()
+// root-expansion sections (thread 0 after a block barrier): cycles, events
+#define PA_MARK(sec)                                                                    \
+    do {                                                                                \
+        if (threadIdx.x == 0 && a.prof_a) {                                             \
+            long long t__ = clock64();                                                  \
+            atomicAdd(&a.prof_a[2 * (sec)], (unsigned long long)(t__ - pa_t));         \
+            atomicAdd(&a.prof_a[2 * (sec) + 1], 1ull);                                  \
+            pa_t = t__;                                                                 \
+        }                                                                               \
+    } while (0)
 #define PROF_VAL(acc_arr, sec, v) do { (acc_arr)[2 * (sec)] += (v); (acc_arr)[2 * (sec) + 1]++; } while (0)
 #define PROF_ADD(acc_arr, sec) do { (acc_arr)[2 * (sec)] += clock64() - prof_t0__; (acc_arr)[2 * (sec) + 1]++; prof_t0__ = clock64(); } while (0)
 #else
 #define PROF_T0() do {} while (0)
 #define PROF_ADD(acc_arr, sec) do {} while (0)
+#define PA_MARK(sec) do {} while (0)
 #define PROF_VAL(acc_arr, sec, v) do {} while (0)
 #define PROF_TAB(cls, c0, v) do {} while (0)
 #endif
@@ -141,27 +152,6 @@ __device__ __forceinline__ uint64_t side_hash(const GraphView& G, uint64_t sL, u
                                               uint32_t nr) {
     // A = rows, B = cols of the file; R is the file's rows unless swapped.
     return G.swapped ? mbe_pair_hash(sL, nl, sR, nr) : mbe_pair_hash(sR, nr, sL, nl);
-}
-
-// ---------------------------------------------------------------------------
-// block-level bitonic sort of u64 keys (n a power of two)
-
-__device__ void block_sort_u64(unsigned long long* k, uint32_t n) {
-    for (uint32_t size = 2; size <= n; size <<= 1)
-        for (uint32_t j = size >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-                uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    unsigned long long x = k[i], y = k[ixj];
-                    bool asc = (i & size) == 0;
-                    if ((x > y) == asc) {
-                        k[i] = y;
-                        k[ixj] = x;
-                    }
-                }
-            }
-            __syncthreads();
-        }
 }
 
 // warp-level bitonic sort of u64 keys in memory (n a power of two >= 32)
@@ -196,6 +186,31 @@ __device__ __forceinline__ unsigned long long warp_sort_reg(unsigned long long v
             v = (lower == up) ? (v < o ? v : o) : (v > o ? v : o);
         }
     return v;
+}
+
+// In-place exclusive prefix sum of a[0..m) by the whole block (each thread
+// a contiguous chunk); s_part holds one word per warp.  Ends with a barrier.
+__device__ void block_exclusive_scan(uint32_t* a, uint32_t m, uint32_t* s_part) {
+    const uint32_t t = threadIdx.x, nt = blockDim.x, lane = t & 31u, warp = t >> 5;
+    const uint32_t ch = (m + nt - 1) / nt, b = min(m, t * ch), e = min(m, b + ch);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += a[i];
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= (uint32_t)o) inc += y;
+    }
+    if (lane == 31) s_part[warp] = inc;
+    __syncthreads();
+    uint32_t run = inc - sum;
+    for (uint32_t w = 0; w < warp; w++) run += s_part[w];
+    for (uint32_t i = b; i < e; i++) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ uint32_t next_pow2(uint32_t x) {
@@ -305,6 +320,10 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
         }
         __syncthreads();
         if (s_stop) break;
+#ifdef MBE_PROFILE
+        long long pa_t = clock64();
+        const long long pa_root0 = pa_t;
+#endif
         const uint2 rt = a.roots[s_idx];
         const GraphView G = a.graphs[rt.x];
         const uint32_t x = rt.y;
@@ -363,29 +382,22 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
             }
         }
         __syncthreads();
+        PA_MARK(0);
         // 3. classify: Q part (lower rank), absorbed, P part
         unsigned long long sabs = 0;
         uint32_t nabs = 0, nq = 0, np = 0, nonmax = 0;
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             uint32_t v = cl[i], c = cntA[i];
-            unsigned long long key;
             if (v < x) {
                 nonmax |= (c == d);
-                key = ((unsigned long long)(0x7FFFFFFFu - c) << 32) | v;  // count desc, rank asc
                 nq++;
             } else if (c == d) {
-                key = kInvalidKey;
                 sabs += G.eR[v];
                 nabs++;
                 cmap[v] = -3;
             } else {
-                key = (1ull << 63) | ((unsigned long long)c << 32) | v;
                 np++;
             }
-            if (n <= 2048)
-                s_keys[i] = key;
-            else
-                gkeys[i] = key;
         }
         sabs = warp_sum(sabs);
         nabs = warp_sum(nabs);
@@ -440,6 +452,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
             }
         }
         __syncthreads();
+        PA_MARK(1);
         if (a.emit && s_counted && warp == 0) {
             // the root biclique: R = x + the absorbed, L = N(x)
             const unsigned long long o = emit_reserve(a, nRset, d, G.swapped);
@@ -451,14 +464,25 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
             }
         }
         if (emit_task && s_rec != ~0ull) {
-            // 4. order: Q part by rank, then P part by (count, rank)
-            uint32_t N = next_pow2(max(n, 2u));
-            unsigned long long* keys = (n <= 2048 && N <= 2048) ? s_keys : gkeys;
-            if (keys == gkeys && n <= 2048)
-                for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) gkeys[i] = s_keys[i];
-            for (uint32_t i = n + threadIdx.x; i < N; i += blockDim.x) keys[i] = kInvalidKey;
+            // 4. order: Q part by count descending, then P part by count
+            // ascending (the min-count child order), by a counting sort over
+            // 2d buckets: a Q count c goes to bucket d - c, a P count c to
+            // bucket d + c.  Candidates of equal count keep no fixed order.
+            uint32_t* hist = 2 * d <= 4096 ? (uint32_t*)s_keys : (uint32_t*)gkeys;
+            for (uint32_t b = threadIdx.x; b < 2 * d; b += blockDim.x) hist[b] = 0;
             __syncthreads();
-            block_sort_u64(keys, N);
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                const uint32_t v = cl[i], c = cntA[i];
+                if (v < x)
+                    atomicAdd(&hist[d - c], 1u);
+                else if (c != d)
+                    atomicAdd(&hist[d + c], 1u);
+            }
+            __syncthreads();
+            block_exclusive_scan(hist, 2 * d, s_wsum);
+#ifdef MBE_PROFILE
+            PA_MARK(2);
+#endif
             {
                 uint32_t* rec = a.pool + s_rec;
                 uint32_t* wmap = rec + kHdrWords;
@@ -487,11 +511,13 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                     uint32_t rem = d - w * 32;
                     Lm[w] = rem >= 32 ? 0xFFFFFFFFu : ((1u << rem) - 1u);
                 }
-                for (uint32_t p = threadIdx.x; p < n2; p += blockDim.x) {
-                    unsigned long long k = keys[p];
-                    uint32_t v = (uint32_t)k;
+                for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                    const uint32_t v = cl[i], c = cntA[i];
+                    const bool q = v < x;
+                    if (!q && c == d) continue;  // absorbed
+                    const uint32_t p = atomicAdd(&hist[q ? d - c : d + c], 1u);
                     cand[p] = v;
-                    cnt[p] = (k >> 63) ? (uint32_t)((k >> 32) & 0x7FFFFFFFu) : 0u;
+                    cnt[p] = q ? 0u : c;
                     cmap[v] = (int)p;
                 }
                 uint64_t mw = (uint64_t)W * n2;
@@ -525,10 +551,11 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                     }
                 }
                 __syncthreads();
+                PA_MARK(3);
                 // 7. Q reduction: a Q row contained in one of the first
                 // kKeepWindow kept rows (Q is in count-descending order) is
                 // dropped; the record is then compacted in place.
-                uint32_t* flag = (uint32_t*)keys;  // keys are consumed: reuse as keep flags
+                uint32_t* flag = s_nq <= 4096 ? (uint32_t*)s_keys : (uint32_t*)gkeys;  // keep flags
                 if (warp == 0) {
                     uint32_t kept_p = 0, nk = 0, pos = 0;
                     while (pos < s_nq && nk < kKeepWindow) {
@@ -554,19 +581,40 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                 }
                 __syncthreads();
                 for (uint32_t p = s_p1 + threadIdx.x; p < s_nq; p += blockDim.x) {
+                    // a Q row meets few of L0's words: find them once (up to
+                    // four), then test the kept rows on those words only
+                    uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, nz = 0;
+                    for (uint32_t w = 0; w < W; w++) {
+                        const uint32_t v = M[(size_t)w * n2 + p];
+                        if (v) {
+                            if (nz == 0) { w0 = w; v0 = v; }
+                            else if (nz == 1) { w1 = w; v1 = v; }
+                            else if (nz == 2) { w2 = w; v2 = v; }
+                            else if (nz == 3) { w3 = w; v3 = v; }
+                            nz++;
+                        }
+                    }
                     bool keep = true;
                     for (uint32_t j = 0; j < s_nk && keep; j++) {
-                        uint32_t kp = s_kept[j];
+                        const uint32_t kp = s_kept[j];
                         bool sub = true;
-                        for (uint32_t w = 0; w < W && sub; w++) {
-                            const uint32_t* Mw = M + (size_t)w * n2;
-                            if (Mw[p] & ~Mw[kp]) sub = false;
+                        if (nz <= 4) {
+                            sub = (v0 & ~M[(size_t)w0 * n2 + kp]) == 0;
+                            if (sub && nz > 1) sub = (v1 & ~M[(size_t)w1 * n2 + kp]) == 0;
+                            if (sub && nz > 2) sub = (v2 & ~M[(size_t)w2 * n2 + kp]) == 0;
+                            if (sub && nz > 3) sub = (v3 & ~M[(size_t)w3 * n2 + kp]) == 0;
+                        } else {
+                            for (uint32_t w = 0; w < W && sub; w++) {
+                                const uint32_t* Mw = M + (size_t)w * n2;
+                                if (Mw[p] & ~Mw[kp]) sub = false;
+                            }
                         }
                         if (sub) keep = false;
                     }
                     flag[p] = keep;
                 }
                 __syncthreads();
+                PA_MARK(4);
                 // new positions of kept Q rows (block scan in chunks)
                 if (threadIdx.x == 0) s_nq2 = 0;
                 __syncthreads();
@@ -653,8 +701,17 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
             }
         }
         __syncthreads();
+        PA_MARK(5);
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) cmap[cl[i]] = -1;
         __syncthreads();
+#ifdef MBE_PROFILE
+        if (threadIdx.x == 0 && a.prof_a) {
+            unsigned long long tot = (unsigned long long)(clock64() - pa_root0);
+            atomicAdd(&a.prof_a[12], tot);
+            atomicAdd(&a.prof_a[13], 1ull);
+            if (tot > atomicMax(&a.prof_a[14], tot)) a.prof_a[15] = d;
+        }
+#endif
     }
 }
 
@@ -2049,12 +2106,15 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     const uint32_t ng = (uint32_t)gs.size();
     results.assign(ng, ResultAcc{});
     if (ng == 0 || roots.empty()) return MBE_OK;
-    uint32_t maxNR = 1, maxW = 1;
+    uint32_t maxNR = 1, maxW = 1, maxRD = 1;
     for (const DeviceGraph* g : gs) {
         maxNR = std::max(maxNR, g->nR);
         maxW = std::max(maxW, (g->max_rdeg + 31) / 32);
+        maxRD = std::max(maxRD, g->max_rdeg);
     }
-    const uint32_t keys_cap = (uint32_t)std::max<size_t>(2048, [&] {
+    // per-block root scratch: keep flags (u32 per candidate) and the count
+    // histogram (2 x degree u32), as u64 words
+    const uint32_t keys_cap = (uint32_t)std::max<size_t>(std::max<size_t>(2048, maxRD + 1), [&] {
         size_t p = 1;
         while (p < maxNR) p <<= 1;
         return p;
@@ -2166,14 +2226,15 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 #ifdef MBE_PROFILE
     static unsigned long long* prof_dev = nullptr;
     static size_t prof_n = 0;
-    if (prof_n < kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC) {
+    if (prof_n < kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC + 16) {
         if (prof_dev) cudaFree(prof_dev);
-        prof_n = kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC;
+        prof_n = kProfSlots + nwarpsB + 2 * kProfBins + 2 * kProfTB * kProfTC + 16;
         MBE_CUDA_TRY(cudaMalloc(&prof_dev, sizeof(unsigned long long) * prof_n));
     }
     MBE_CUDA_TRY(cudaMemsetAsync(prof_dev, 0, sizeof(unsigned long long) * prof_n, s));
     a.prof = prof_dev;
     a.prof_warps = nwarpsB;
+    a.prof_a = prof_dev + prof_n - 16;
 #endif
 
     cudaEvent_t e0, e1, e2;
@@ -2351,6 +2412,16 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         std::vector<unsigned long long> tab(2 * kProfTB * kProfTC);
         MBE_CUDA_TRY(cudaMemcpy(tab.data(), a.prof + kProfSlots + nwarpsB + 2 * kProfBins,
                                 sizeof(unsigned long long) * tab.size(), cudaMemcpyDeviceToHost));
+        {
+            unsigned long long pa[16];
+            MBE_CUDA_TRY(cudaMemcpy(pa, a.prof_a, sizeof pa, cudaMemcpyDeviceToHost));
+            static const char* an[] = {"discover+count", "classify", "sort", "rows", "reduce", "compact+push"};
+            std::fprintf(stderr, "profA roots %llu total Gcycles %.2f; max root %.2f Mcycles (degree %llu)\n", pa[13],
+                         pa[12] / 1e9, pa[14] / 1e6, pa[15]);
+            for (int q = 0; q < 6; q++)
+                std::fprintf(stderr, "profA %-15s Gcycles %8.3f (%5.1f%%) events %llu\n", an[q], pa[2 * q] / 1e9,
+                             pa[12] ? 100.0 * pa[2 * q] / pa[12] : 0.0, pa[2 * q + 1]);
+        }
         std::fprintf(stderr, "prof eval table: per 64 ms, class W1 W2 W4 W8 W16 W32 W64 W128+ replay prefilter: "
                              "Gcycles/evals; avg depth\n");
         for (int b = 0; b < kProfTB; b++) {

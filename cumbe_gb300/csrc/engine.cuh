@@ -187,6 +187,7 @@ struct EngineArgs {
     // section cycle counters (builds with -DMBE_PROFILE only; else null)
     unsigned long long* prof;  // [kProfSlots + warps + 2 * kProfBins]
     uint32_t prof_warps;
+    unsigned long long* prof_a;  // [16] root-expansion sections (profile builds)
     // output stream (MBE_OPT_EMIT; emit == 0 otherwise): each counted
     // biclique reserves room for its file rows then its file cols
     uint32_t emit;
