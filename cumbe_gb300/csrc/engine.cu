@@ -188,6 +188,42 @@ __device__ __forceinline__ unsigned long long warp_sort_reg(unsigned long long v
     return v;
 }
 
+// A row of a root record (word-major rows, n2 of them) by its first four
+// non-zero words; most candidate rows meet only a few words of N(x).
+struct SparseRow {
+    uint32_t w0, w1, w2, w3, v0, v1, v2, v3, nz;
+};
+
+__device__ __forceinline__ SparseRow sparse_row(const uint32_t* M, uint32_t n2, uint32_t W, uint32_t p) {
+    SparseRow r{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t w = 0; w < W; w++) {
+        const uint32_t v = M[(size_t)w * n2 + p];
+        if (v) {
+            if (r.nz == 0) { r.w0 = w; r.v0 = v; }
+            else if (r.nz == 1) { r.w1 = w; r.v1 = v; }
+            else if (r.nz == 2) { r.w2 = w; r.v2 = v; }
+            else if (r.nz == 3) { r.w3 = w; r.v3 = v; }
+            r.nz++;
+        }
+    }
+    return r;
+}
+
+// Row p (described by r) is a subset of row q.
+__device__ __forceinline__ bool row_subset(const SparseRow& r, const uint32_t* M, uint32_t n2, uint32_t W,
+                                           uint32_t p, uint32_t q) {
+    if (r.nz > 4) {
+        for (uint32_t w = 0; w < W; w++)
+            if (M[(size_t)w * n2 + p] & ~M[(size_t)w * n2 + q]) return false;
+        return true;
+    }
+    if (r.nz > 0 && (r.v0 & ~M[(size_t)r.w0 * n2 + q])) return false;
+    if (r.nz > 1 && (r.v1 & ~M[(size_t)r.w1 * n2 + q])) return false;
+    if (r.nz > 2 && (r.v2 & ~M[(size_t)r.w2 * n2 + q])) return false;
+    if (r.nz > 3 && (r.v3 & ~M[(size_t)r.w3 * n2 + q])) return false;
+    return true;
+}
+
 // In-place exclusive prefix sum of a[0..m) by the whole block (each thread
 // a contiguous chunk); s_part holds one word per warp.  Ends with a barrier.
 __device__ void block_exclusive_scan(uint32_t* a, uint32_t m, uint32_t* s_part) {
@@ -557,60 +593,50 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
                 // dropped; the record is then compacted in place.
                 uint32_t* flag = s_nq <= 4096 ? (uint32_t*)s_keys : (uint32_t*)gkeys;  // keep flags
                 if (warp == 0) {
+                    // kept window: greedy in row order, 32 rows per step.  Each
+                    // lane tests its row against the window; survivors are
+                    // taken in order and each one kept is tested against by
+                    // the later lanes (same result as one row at a time).
                     uint32_t kept_p = 0, nk = 0, pos = 0;
                     while (pos < s_nq && nk < kKeepWindow) {
-                        bool dom = false;
-                        if (lane < nk) {
-                            dom = true;
-                            for (uint32_t w = 0; w < W && dom; w++) {
-                                const uint32_t* Mw = M + (size_t)w * n2;
-                                if (Mw[pos] & ~Mw[kept_p]) dom = false;
-                            }
+                        const uint32_t p = pos + lane;
+                        const bool valid = p < s_nq;
+                        const SparseRow r = sparse_row(M, n2, W, valid ? p : pos);
+                        bool dom = !valid;
+                        for (uint32_t j = 0; j < nk; j++) {
+                            const uint32_t kp = __shfl_sync(kFull, kept_p, j);
+                            dom = dom || row_subset(r, M, n2, W, p, kp);
                         }
-                        bool keep = !__any_sync(kFull, dom);
-                        if (keep && lane == nk) kept_p = pos;
-                        if (lane == 0) flag[pos] = keep;
-                        nk += keep;
-                        pos++;
+                        unsigned pending = __ballot_sync(kFull, !dom), keepm = 0;
+                        uint32_t upto = 32;  // lanes whose row this step decides
+                        while (pending) {
+                            const uint32_t j = __ffs(pending) - 1;
+                            pending &= pending - 1;
+                            if (nk == kKeepWindow) {  // window full: the rest go to the parallel pass
+                                upto = j;
+                                break;
+                            }
+                            keepm |= 1u << j;
+                            if (lane == nk) kept_p = pos + j;
+                            nk++;
+                            pending &= ~__ballot_sync(kFull, lane > j && ((pending >> lane) & 1u) &&
+                                                                 row_subset(r, M, n2, W, p, pos + j));
+                        }
+                        if (valid && lane < upto) flag[p] = (keepm >> lane) & 1u;
+                        pos += upto;
                     }
                     if (lane < nk) s_kept[lane] = kept_p;
                     if (lane == 0) {
                         s_nk = nk;
-                        s_p1 = pos;
+                        s_p1 = min(pos, s_nq);
                     }
                 }
                 __syncthreads();
                 for (uint32_t p = s_p1 + threadIdx.x; p < s_nq; p += blockDim.x) {
-                    // a Q row meets few of L0's words: find them once (up to
-                    // four), then test the kept rows on those words only
-                    uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, nz = 0;
-                    for (uint32_t w = 0; w < W; w++) {
-                        const uint32_t v = M[(size_t)w * n2 + p];
-                        if (v) {
-                            if (nz == 0) { w0 = w; v0 = v; }
-                            else if (nz == 1) { w1 = w; v1 = v; }
-                            else if (nz == 2) { w2 = w; v2 = v; }
-                            else if (nz == 3) { w3 = w; v3 = v; }
-                            nz++;
-                        }
-                    }
+                    const SparseRow r = sparse_row(M, n2, W, p);
                     bool keep = true;
-                    for (uint32_t j = 0; j < s_nk && keep; j++) {
-                        const uint32_t kp = s_kept[j];
-                        bool sub = true;
-                        if (nz <= 4) {
-                            sub = (v0 & ~M[(size_t)w0 * n2 + kp]) == 0;
-                            if (sub && nz > 1) sub = (v1 & ~M[(size_t)w1 * n2 + kp]) == 0;
-                            if (sub && nz > 2) sub = (v2 & ~M[(size_t)w2 * n2 + kp]) == 0;
-                            if (sub && nz > 3) sub = (v3 & ~M[(size_t)w3 * n2 + kp]) == 0;
-                        } else {
-                            for (uint32_t w = 0; w < W && sub; w++) {
-                                const uint32_t* Mw = M + (size_t)w * n2;
-                                if (Mw[p] & ~Mw[kp]) sub = false;
-                            }
-                        }
-                        if (sub) keep = false;
-                    }
+                    for (uint32_t j = 0; j < s_nk && keep; j++)
+                        if (row_subset(r, M, n2, W, p, s_kept[j])) keep = false;
                     flag[p] = keep;
                 }
                 __syncthreads();
