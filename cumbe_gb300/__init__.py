@@ -87,6 +87,9 @@ SIGNATURES = {
     "mbe_graph_from_csr": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, _U64P, _U32P, ctypes.POINTER(_VP)]),
     "mbe_graph_generate": (ctypes.c_int, [ctypes.POINTER(_GenParams), ctypes.POINTER(_VP)]),
     "mbe_graph_write_bi": (ctypes.c_int, [_VP, ctypes.c_char_p]),
+    "mbe_graph_write_bin": (ctypes.c_int, [_VP, ctypes.c_char_p]),
+    "mbe_graph_load_bin": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "mbe_graph_load_cached": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_VP)]),
     "mbe_graph_info_get": (ctypes.c_int, [_VP, ctypes.POINTER(_GraphInfo)]),
     "mbe_graph_copy_csr": (ctypes.c_int, [_VP, _U64P, _U32P]),
     "mbe_graph_free": (None, [_VP]),
@@ -213,6 +216,24 @@ class Graph:
 
     def write_bi(self, path: str):
         _check(lib().mbe_graph_write_bi(self._h, os.fsencode(path)), "mbe_graph_write_bi")
+
+    def write_bin(self, path: str):
+        """Binary graph image (checksummed normalised CSR)."""
+        _check(lib().mbe_graph_write_bin(self._h, os.fsencode(path)), "mbe_graph_write_bin")
+
+    @classmethod
+    def load_bin(cls, path: str) -> "Graph":
+        h = _VP()
+        _check(lib().mbe_graph_load_bin(os.fsencode(path), ctypes.byref(h)), "mbe_graph_load_bin")
+        return cls(h)
+
+    @classmethod
+    def load_cached(cls, bi_path: str, cache_path: str) -> "Graph":
+        """`.bi` file through a binary cache (reused while at least as new)."""
+        h = _VP()
+        _check(lib().mbe_graph_load_cached(os.fsencode(bi_path), os.fsencode(cache_path), ctypes.byref(h)),
+               "mbe_graph_load_cached")
+        return cls(h)
 
 
 def _opts(flags=0, min_rows=0, min_cols=0, donate_min=0, blocks_per_sm=0, stack_words=0) -> _Opts:

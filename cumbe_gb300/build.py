@@ -83,7 +83,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or not os.path.exists(LIB):
-        subprocess.check_call([nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs)
+        subprocess.check_call([nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lpthread"])
         os.replace(LIB + ".tmp", LIB)
     cli_src = os.path.join(CSRC, "mbe_cli.cpp")
     if force or _stale(CLI, [cli_src, LIB]):

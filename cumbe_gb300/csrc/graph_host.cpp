@@ -1,6 +1,9 @@
 // Host-side graph handling of libmbe: `.bi` reader and writer, CSR ingest,
-// and the synthetic bipartite generator.  No CUDA calls here, so every
-// function works on a machine without a GPU.
+// the binary graph image and cache, and the synthetic bipartite generator.
+// No CUDA calls here, so every function works on a machine without a GPU.
+// Large inputs are parsed and normalised on all host threads.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -8,6 +11,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mbe_hash.h"
@@ -29,38 +33,105 @@ uint64_t next_graph_uid() {
     return ctr.fetch_add(1);
 }
 
-mbe_status normalise(mbe_graph* g) {
-    g->n_dup = 0;
-    g->max_row_deg = 0;
-    std::vector<uint32_t> col_deg(g->n_cols, 0);
-    uint64_t w = 0;
-    for (uint32_t r = 0; r < g->n_rows; r++) {
-        uint64_t b = g->row_ptr[r], e = g->row_ptr[r + 1];
-        auto first = g->col_idx.begin() + (ptrdiff_t)b;
-        auto last = g->col_idx.begin() + (ptrdiff_t)e;
-        for (auto it = first; it != last; ++it)
-            if (*it >= g->n_cols)
-                return fail(MBE_ERR_FORMAT, "column id " + std::to_string(*it) + " out of range in row " +
-                                                std::to_string(r));
-        std::sort(first, last);
-        auto uend = std::unique(first, last);
-        uint64_t len = (uint64_t)(uend - first);
-        g->n_dup += (uint32_t)((e - b) - len);
-        // compact in place (w <= b always holds)
-        for (uint64_t i = 0; i < len; i++) {
-            uint32_t c = g->col_idx[b + i];
-            g->col_idx[w + i] = c;
-            col_deg[c]++;
-        }
-        g->row_ptr[r] = w;
-        w += len;
-        if (len > g->max_row_deg) g->max_row_deg = (uint32_t)len;
+namespace {
+
+// Host threads for a job over `work` items (1 below `min_work`).
+unsigned worker_count(uint64_t work, uint64_t min_work) {
+    if (work < min_work) return 1;
+    unsigned hw = std::thread::hardware_concurrency();
+    return std::max(1u, std::min(hw ? hw : 1u, 32u));
+}
+
+// Runs f(t) for t in [0, n) on n threads (the calling thread takes t = 0).
+template <class F>
+void run_threads(unsigned n, F f) {
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < n; t++) th.emplace_back(f, t);
+    f(0u);
+    for (auto& x : th) x.join();
+}
+
+// Row ranges [cut[t], cut[t+1]) holding about equal numbers of edges.
+std::vector<uint32_t> row_cuts(const std::vector<uint64_t>& row_ptr, uint32_t n_rows, unsigned T) {
+    std::vector<uint32_t> cut(T + 1, n_rows);
+    cut[0] = 0;
+    const uint64_t E = row_ptr[n_rows];
+    for (unsigned t = 1; t < T; t++) {
+        const uint64_t target = E * t / T;
+        cut[t] = (uint32_t)(std::lower_bound(row_ptr.begin(), row_ptr.begin() + n_rows + 1, target) - row_ptr.begin());
+        cut[t] = std::max(cut[t], cut[t - 1]);
     }
-    g->row_ptr[g->n_rows] = w;
-    g->col_idx.resize(w);
-    g->col_idx.shrink_to_fit();
-    g->max_col_deg = 0;
-    for (uint32_t c : col_deg) g->max_col_deg = std::max(g->max_col_deg, c);
+    return cut;
+}
+
+}  // namespace
+
+// Sorts and dedupes every row, checks column ids, fills the degree maxima.
+// Rows are processed on all host threads for large graphs; the first row
+// (in row order) holding a bad id is the one reported.
+mbe_status normalise(mbe_graph* g) {
+    const uint32_t nr = g->n_rows, nc = g->n_cols;
+    const unsigned T = worker_count(g->col_idx.size(), 1u << 20);
+    const std::vector<uint32_t> cut = row_cuts(g->row_ptr, nr, T);
+    std::vector<uint64_t> newlen((size_t)nr + 1, 0);
+    std::vector<uint32_t> bad_row(T, UINT32_MAX);
+    run_threads(T, [&](unsigned t) {
+        for (uint32_t r = cut[t]; r < cut[t + 1]; r++) {
+            auto first = g->col_idx.begin() + (ptrdiff_t)g->row_ptr[r];
+            auto last = g->col_idx.begin() + (ptrdiff_t)g->row_ptr[r + 1];
+            for (auto it = first; it != last; ++it)
+                if (*it >= nc) {
+                    bad_row[t] = r;
+                    return;
+                }
+            std::sort(first, last);
+            newlen[r] = (uint64_t)(std::unique(first, last) - first);
+        }
+    });
+    for (unsigned t = 0; t < T; t++)
+        if (bad_row[t] != UINT32_MAX) {
+            const uint32_t r = bad_row[t];
+            uint32_t c = 0;
+            for (uint64_t i = g->row_ptr[r]; i < g->row_ptr[r + 1]; i++)
+                if (g->col_idx[i] >= nc) {
+                    c = g->col_idx[i];
+                    break;
+                }
+            return fail(MBE_ERR_FORMAT, "column id " + std::to_string(c) + " out of range in row " + std::to_string(r));
+        }
+    // new offsets (serial prefix over rows), then compaction and column
+    // degrees per thread
+    std::vector<uint64_t> np((size_t)nr + 1, 0);
+    uint64_t w = 0, dup = 0;
+    uint32_t maxr = 0;
+    for (uint32_t r = 0; r < nr; r++) {
+        np[r] = w;
+        w += newlen[r];
+        dup += (g->row_ptr[r + 1] - g->row_ptr[r]) - newlen[r];
+        maxr = std::max<uint32_t>(maxr, (uint32_t)newlen[r]);
+    }
+    np[nr] = w;
+    std::vector<uint32_t> out(w);
+    std::vector<std::vector<uint32_t>> deg(T);
+    run_threads(T, [&](unsigned t) {
+        deg[t].assign(nc, 0);
+        for (uint32_t r = cut[t]; r < cut[t + 1]; r++) {
+            const uint32_t* src = g->col_idx.data() + g->row_ptr[r];
+            if (newlen[r]) std::memcpy(out.data() + np[r], src, sizeof(uint32_t) * newlen[r]);
+            for (uint64_t i = 0; i < newlen[r]; i++) deg[t][src[i]]++;
+        }
+    });
+    uint32_t maxc = 0;
+    for (uint32_t c = 0; c < nc; c++) {
+        uint32_t d = 0;
+        for (unsigned t = 0; t < T; t++) d += deg[t][c];
+        maxc = std::max(maxc, d);
+    }
+    g->row_ptr.swap(np);
+    g->col_idx.swap(out);
+    g->n_dup = (uint32_t)std::min<uint64_t>(dup, UINT32_MAX);
+    g->max_row_deg = maxr;
+    g->max_col_deg = maxc;
     return MBE_OK;
 }
 
@@ -93,6 +164,191 @@ struct Scanner {
     }
 };
 
+inline bool is_ws(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t'; }
+
+// One whitespace-delimited token [b, e) read like Scanner::next: optional
+// sign, decimal digits, at most 2^40.
+inline bool parse_token(const char* b, const char* e, long long* out) {
+    bool neg = false;
+    if (b < e && (*b == '-' || *b == '+')) {
+        neg = *b == '-';
+        b++;
+    }
+    if (b >= e) return false;
+    long long v = 0;
+    for (; b < e; b++) {
+        if (*b < '0' || *b > '9') return false;
+        v = v * 10 + (*b - '0');
+        if (v > (1LL << 40)) return false;
+    }
+    *out = neg ? -v : v;
+    return true;
+}
+
+// Parses a `.bi` image (src/main.cu:38-48 reads the same layout: header
+// "R L E", R lines "start len", E lines "neighbour ignored") into a
+// normalised graph.  After the header, the text is cut at whitespace into
+// one chunk per host thread; a first pass counts each chunk's tokens, a
+// second parses every token straight into its slot (row table or edge
+// list).  Errors name the same row / edge as a sequential read would.
+mbe_status parse_bi(const char* data, size_t size, mbe_graph** out) {
+    Scanner sc{data, data + size};
+    long long nr, nl, ne;
+    if (!sc.next(&nr) || !sc.next(&nl) || !sc.next(&ne)) return fail(MBE_ERR_FORMAT, "missing header 'R L E'");
+    if (nr < 0 || nl < 0 || ne < 0 || nr > 0xFFFFFFFFLL || nl > 0xFFFFFFFFLL)
+        return fail(MBE_ERR_FORMAT, "bad header values");
+    const char* p0 = sc.p;
+    const char* end = data + size;
+    const uint64_t want = 2ull * (uint64_t)nr + 2ull * (uint64_t)ne;  // tokens after the header
+    const unsigned T = worker_count((uint64_t)(end - p0), 8u << 20);
+    std::vector<const char*> cut(T + 1);
+    cut[0] = p0;
+    cut[T] = end;
+    for (unsigned k = 1; k < T; k++) {
+        const char* c = p0 + (size_t)(end - p0) * k / T;
+        while (c < end && !is_ws(*c)) c++;
+        cut[k] = std::max(c, cut[k - 1]);
+    }
+    // pass 1: tokens per chunk (a chunk starts at whitespace, or right after the header)
+    std::vector<uint64_t> first(T + 1, 0);
+    run_threads(T, [&](unsigned t) {
+        uint64_t n = 0;
+        bool in = false;
+        for (const char* c = cut[t]; c < cut[t + 1]; c++) {
+            const bool w = is_ws(*c);
+            n += (!w && !in);
+            in = !w;
+        }
+        first[t + 1] = n;
+    });
+    for (unsigned t = 0; t < T; t++) first[t + 1] += first[t];
+    const uint64_t total = first[T];
+    std::vector<long long> start((size_t)nr), len((size_t)nr);
+    std::vector<uint32_t> edges((size_t)ne);
+    std::vector<uint64_t> bad_tok(T, UINT64_MAX), bad_nbr(T, UINT64_MAX);
+    // pass 2: every token into its slot
+    run_threads(T, [&](unsigned t) {
+        uint64_t idx = first[t];
+        const char* c = cut[t];
+        const char* ce = cut[t + 1];
+        while (c < ce && idx < want) {
+            while (c < ce && is_ws(*c)) c++;
+            if (c >= ce) break;
+            const char* b = c;
+            while (c < ce && !is_ws(*c)) c++;
+            long long v;
+            if (!parse_token(b, c, &v)) {
+                bad_tok[t] = idx;
+                return;
+            }
+            if (idx < 2ull * (uint64_t)nr) {
+                (idx & 1 ? len : start)[(size_t)(idx >> 1)] = v;
+            } else {
+                const uint64_t u = idx - 2ull * (uint64_t)nr;
+                if (!(u & 1)) {
+                    if (v < 0 || v >= nl) {
+                        if (bad_nbr[t] == UINT64_MAX) bad_nbr[t] = u >> 1;
+                    } else {
+                        edges[(size_t)(u >> 1)] = (uint32_t)v;
+                    }
+                }
+            }
+            idx++;
+        }
+    });
+    uint64_t tok_err = total < want ? total : UINT64_MAX, nbr_err = UINT64_MAX;
+    for (unsigned t = 0; t < T; t++) {
+        tok_err = std::min(tok_err, bad_tok[t]);
+        nbr_err = std::min(nbr_err, bad_nbr[t]);
+    }
+    // the row table, in the order a sequential read reports problems
+    const uint64_t rows_ok = tok_err < 2ull * (uint64_t)nr ? tok_err / 2 : (uint64_t)nr;
+    for (uint64_t i = 0; i < rows_ok; i++)
+        if (start[i] < 0 || len[i] < 0 || start[i] + len[i] > ne)
+            return fail(MBE_ERR_FORMAT, "row " + std::to_string(i) + " range outside edge list");
+    if (tok_err < 2ull * (uint64_t)nr)
+        return fail(MBE_ERR_FORMAT, "truncated row table at row " + std::to_string(tok_err / 2));
+    const uint64_t edge_tok_err = tok_err == UINT64_MAX ? UINT64_MAX : (tok_err - 2ull * (uint64_t)nr) / 2;
+    if (edge_tok_err != UINT64_MAX && edge_tok_err <= nbr_err)
+        return fail(MBE_ERR_FORMAT, "truncated edge list at edge " + std::to_string(edge_tok_err));
+    if (nbr_err != UINT64_MAX)
+        return fail(MBE_ERR_FORMAT, "neighbour id out of range at edge " + std::to_string(nbr_err));
+    auto* g = new (std::nothrow) mbe_graph();
+    if (!g) return fail(MBE_ERR_OUT_OF_MEMORY, "host allocation failed");
+    g->n_rows = (uint32_t)nr;
+    g->n_cols = (uint32_t)nl;
+    g->row_ptr.assign((size_t)nr + 1, 0);
+    uint64_t tot = 0;
+    for (long long i = 0; i < nr; i++) {
+        g->row_ptr[(size_t)i] = tot;
+        tot += (uint64_t)len[(size_t)i];
+    }
+    g->row_ptr[(size_t)nr] = tot;
+    g->col_idx.resize(tot);
+    const std::vector<uint32_t> rc = row_cuts(g->row_ptr, (uint32_t)nr, worker_count(tot, 1u << 20));
+    run_threads((unsigned)rc.size() - 1, [&](unsigned t) {
+        for (uint32_t i = rc[t]; i < rc[t + 1]; i++)
+            if (len[i])
+                std::memcpy(g->col_idx.data() + g->row_ptr[i], edges.data() + start[i], sizeof(uint32_t) * (size_t)len[i]);
+    });
+    mbe_status st = normalise(g);
+    if (st != MBE_OK) {
+        delete g;
+        return st;
+    }
+    g->uid = next_graph_uid();
+    *out = g;
+    return MBE_OK;
+}
+
+mbe_status read_file(const char* path, std::vector<char>& buf) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(MBE_ERR_IO, std::string("cannot open ") + path);
+    std::fseek(f, 0, SEEK_END);
+    long sz = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (sz < 0) {
+        std::fclose(f);
+        return fail(MBE_ERR_IO, "cannot size file");
+    }
+    buf.resize((size_t)sz);
+    size_t got = sz ? std::fread(buf.data(), 1, (size_t)sz, f) : 0;
+    std::fclose(f);
+    if (got != (size_t)sz) return fail(MBE_ERR_IO, "short read");
+    return MBE_OK;
+}
+
+// Binary graph image: this header, then row_ptr (u64 x (n_rows + 1)), then
+// col_idx (u32 x n_edges), little-endian, rows already normalised.
+struct BinHeader {
+    char magic[8];
+    uint32_t n_rows, n_cols;
+    uint64_t n_edges;
+    uint32_t max_row_deg, max_col_deg, n_dup, version;
+    uint64_t checksum;
+};
+static_assert(sizeof(BinHeader) == 48, "binary header size");
+constexpr char kBinMagic[8] = {'M', 'B', 'E', 'G', 'R', 'A', 'P', 'H'};
+constexpr uint32_t kBinVersion = 1;
+
+// Order-independent checksum of the two arrays (wrapping sum of mixed
+// (position, value) pairs), computed on all host threads.
+uint64_t image_checksum(const std::vector<uint64_t>& rp, const std::vector<uint32_t>& ci) {
+    const unsigned T = worker_count(rp.size() + ci.size(), 1u << 20);
+    std::vector<uint64_t> part(T, 0);
+    run_threads(T, [&](unsigned t) {
+        uint64_t h = 0;
+        for (size_t i = rp.size() * t / T; i < rp.size() * (t + 1) / T; i++)
+            h += mbe_fmix64(rp[i] ^ (0x9E3779B97F4A7C15ull * (i + 1)));
+        for (size_t i = ci.size() * t / T; i < ci.size() * (t + 1) / T; i++)
+            h += mbe_fmix64(((uint64_t)ci[i] << 1) ^ (0xD1B54A32D192ED03ull * (i + 1)));
+        part[t] = h;
+    });
+    uint64_t h = 0;
+    for (uint64_t x : part) h += x;
+    return h;
+}
+
 }  // namespace
 }  // namespace mbe
 
@@ -102,65 +358,104 @@ extern "C" mbe_status mbe_graph_load_bi(const char* path, mbe_graph** out) {
     clear_error();
     if (!path || !out) return fail(MBE_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return fail(MBE_ERR_IO, std::string("cannot open ") + path);
     std::vector<char> buf;
-    {
-        std::fseek(f, 0, SEEK_END);
-        long sz = std::ftell(f);
-        std::fseek(f, 0, SEEK_SET);
-        if (sz < 0) {
-            std::fclose(f);
-            return fail(MBE_ERR_IO, "cannot size file");
-        }
-        buf.resize((size_t)sz);
-        size_t got = sz ? std::fread(buf.data(), 1, (size_t)sz, f) : 0;
-        std::fclose(f);
-        if (got != (size_t)sz) return fail(MBE_ERR_IO, "short read");
+    mbe_status st = read_file(path, buf);
+    if (st != MBE_OK) return st;
+    return parse_bi(buf.data(), buf.size(), out);
+}
+
+extern "C" mbe_status mbe_graph_write_bin(const mbe_graph* g, const char* path) {
+    clear_error();
+    if (!g || !path) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    BinHeader h;
+    std::memcpy(h.magic, kBinMagic, 8);
+    h.n_rows = g->n_rows;
+    h.n_cols = g->n_cols;
+    h.n_edges = g->col_idx.size();
+    h.max_row_deg = g->max_row_deg;
+    h.max_col_deg = g->max_col_deg;
+    h.n_dup = g->n_dup;
+    h.version = kBinVersion;
+    h.checksum = image_checksum(g->row_ptr, g->col_idx);
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return fail(MBE_ERR_IO, std::string("cannot open ") + tmp);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
+              std::fwrite(g->row_ptr.data(), sizeof(uint64_t), g->row_ptr.size(), f) == g->row_ptr.size() &&
+              (g->col_idx.empty() ||
+               std::fwrite(g->col_idx.data(), sizeof(uint32_t), g->col_idx.size(), f) == g->col_idx.size());
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return fail(MBE_ERR_IO, std::string("cannot write ") + path);
     }
-    Scanner sc{buf.data(), buf.data() + buf.size()};
-    long long nr, nl, ne;
-    if (!sc.next(&nr) || !sc.next(&nl) || !sc.next(&ne))
-        return fail(MBE_ERR_FORMAT, "missing header 'R L E'");
-    if (nr < 0 || nl < 0 || ne < 0 || nr > 0xFFFFFFFFLL || nl > 0xFFFFFFFFLL)
-        return fail(MBE_ERR_FORMAT, "bad header values");
-    std::vector<long long> start((size_t)nr), len((size_t)nr);
-    for (long long i = 0; i < nr; i++) {
-        if (!sc.next(&start[(size_t)i]) || !sc.next(&len[(size_t)i]))
-            return fail(MBE_ERR_FORMAT, "truncated row table at row " + std::to_string(i));
-        if (start[(size_t)i] < 0 || len[(size_t)i] < 0 || start[(size_t)i] + len[(size_t)i] > ne)
-            return fail(MBE_ERR_FORMAT, "row " + std::to_string(i) + " range outside edge list");
-    }
-    std::vector<uint32_t> edges((size_t)ne);
-    for (long long i = 0; i < ne; i++) {
-        long long nbr, ignored;
-        if (!sc.next(&nbr) || !sc.next(&ignored))
-            return fail(MBE_ERR_FORMAT, "truncated edge list at edge " + std::to_string(i));
-        if (nbr < 0 || nbr >= nl) return fail(MBE_ERR_FORMAT, "neighbour id out of range at edge " + std::to_string(i));
-        edges[(size_t)i] = (uint32_t)nbr;
-    }
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_graph_load_bin(const char* path, mbe_graph** out) {
+    clear_error();
+    if (!path || !out) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    std::vector<char> buf;
+    mbe_status st = read_file(path, buf);
+    if (st != MBE_OK) return st;
+    BinHeader h;
+    if (buf.size() < sizeof h) return fail(MBE_ERR_FORMAT, "not a binary graph image (too short)");
+    std::memcpy(&h, buf.data(), sizeof h);
+    if (std::memcmp(h.magic, kBinMagic, 8) != 0) return fail(MBE_ERR_FORMAT, "not a binary graph image");
+    if (h.version != kBinVersion) return fail(MBE_ERR_FORMAT, "unsupported binary graph version");
+    const uint64_t need = sizeof h + 8ull * ((uint64_t)h.n_rows + 1) + 4ull * h.n_edges;
+    if (buf.size() != need) return fail(MBE_ERR_FORMAT, "binary graph image has the wrong size");
     auto* g = new (std::nothrow) mbe_graph();
     if (!g) return fail(MBE_ERR_OUT_OF_MEMORY, "host allocation failed");
-    g->n_rows = (uint32_t)nr;
-    g->n_cols = (uint32_t)nl;
-    g->row_ptr.assign((size_t)nr + 1, 0);
-    uint64_t tot = 0;
-    for (long long i = 0; i < nr; i++) tot += (uint64_t)len[(size_t)i];
-    g->col_idx.resize(tot);
-    uint64_t w = 0;
-    for (long long i = 0; i < nr; i++) {
-        g->row_ptr[(size_t)i] = w;
-        std::memcpy(g->col_idx.data() + w, edges.data() + start[(size_t)i], sizeof(uint32_t) * (size_t)len[(size_t)i]);
-        w += (uint64_t)len[(size_t)i];
+    g->n_rows = h.n_rows;
+    g->n_cols = h.n_cols;
+    g->row_ptr.resize((size_t)h.n_rows + 1);
+    g->col_idx.resize((size_t)h.n_edges);
+    std::memcpy(g->row_ptr.data(), buf.data() + sizeof h, 8 * g->row_ptr.size());
+    if (h.n_edges) std::memcpy(g->col_idx.data(), buf.data() + sizeof h + 8 * g->row_ptr.size(), 4 * g->col_idx.size());
+    // checksum, then the CSR invariants the kernels rely on
+    bool ok = image_checksum(g->row_ptr, g->col_idx) == h.checksum && g->row_ptr[0] == 0 &&
+              g->row_ptr[h.n_rows] == h.n_edges;
+    for (uint32_t r = 0; ok && r < h.n_rows; r++) ok = g->row_ptr[r] <= g->row_ptr[r + 1];
+    if (ok) {
+        const unsigned T = worker_count(h.n_edges, 1u << 20);
+        const std::vector<uint32_t> cut = row_cuts(g->row_ptr, h.n_rows, T);
+        std::vector<char> good(T, 1);
+        run_threads(T, [&](unsigned t) {
+            for (uint32_t r = cut[t]; r < cut[t + 1] && good[t]; r++)
+                for (uint64_t i = g->row_ptr[r]; i < g->row_ptr[r + 1]; i++)
+                    if (g->col_idx[i] >= h.n_cols || (i > g->row_ptr[r] && g->col_idx[i] <= g->col_idx[i - 1])) {
+                        good[t] = 0;
+                        break;
+                    }
+        });
+        for (char c : good) ok = ok && c;
     }
-    g->row_ptr[(size_t)nr] = w;
-    mbe_status st = normalise(g);
-    if (st != MBE_OK) {
+    if (!ok) {
         delete g;
-        return st;
+        return fail(MBE_ERR_FORMAT, "binary graph image is corrupt");
     }
+    g->max_row_deg = h.max_row_deg;
+    g->max_col_deg = h.max_col_deg;
+    g->n_dup = h.n_dup;
     g->uid = next_graph_uid();
     *out = g;
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_graph_load_cached(const char* bi_path, const char* cache_path, mbe_graph** out) {
+    clear_error();
+    if (!bi_path || !cache_path || !out) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    struct stat sb, sc;
+    if (stat(bi_path, &sb) != 0) return fail(MBE_ERR_IO, std::string("cannot open ") + bi_path);
+    if (stat(cache_path, &sc) == 0 && sc.st_mtime >= sb.st_mtime && mbe_graph_load_bin(cache_path, out) == MBE_OK)
+        return MBE_OK;
+    mbe_status st = mbe_graph_load_bi(bi_path, out);
+    if (st != MBE_OK) return st;
+    mbe_graph_write_bin(*out, cache_path);  // best effort: the graph is loaded either way
+    clear_error();
     return MBE_OK;
 }
 

@@ -6,6 +6,9 @@
 // device time split.  Exit status is non-zero on any error (the reference
 // ignores errors and prints a count of 0, src/main.cu:185-207).
 //
+// The graph may also be a binary graph image (mbe_graph_write_bin),
+// recognised by its magic.
+//
 // `--emit FILE` (no reference counterpart; the reference only counts) also
 // writes every maximal biclique to FILE, one per line: its rows, " | ",
 // its cols, each side in ascending file ids.  stdout is unchanged.
@@ -88,7 +91,14 @@ int main(int argc, char** argv) {
     std::string stem = dataset.substr(0, dataset.rfind('.'));
 
     mbe_graph* g = nullptr;
-    mbe_status st = mbe_graph_load_bi(pos[0], &g);
+    // a binary graph image (mbe_graph_write_bin) is taken in place of the text
+    bool image = false;
+    if (FILE* f = std::fopen(pos[0], "rb")) {
+        char magic[8] = {0};
+        image = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "MBEGRAPH", 8) == 0;
+        std::fclose(f);
+    }
+    mbe_status st = image ? mbe_graph_load_bin(pos[0], &g) : mbe_graph_load_bi(pos[0], &g);
     if (st != MBE_OK) return die("loading the graph", st);
     mbe_graph_info info;
     mbe_graph_info_get(g, &info);

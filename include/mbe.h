@@ -152,7 +152,8 @@ typedef struct mbe_result {
  * "nbr x" with the second token ignored (src/main.cu:38-48).  Row lists
  * are sorted and deduplicated (the reference's own files hold unsorted
  * lists, data/gen_bi.cpp:78).  Replaces the ifstream reader at
- * src/main.cu:38-48. */
+ * src/main.cu:38-48; large files are parsed and normalised on all host
+ * threads. */
 MBE_API mbe_status mbe_graph_load_bi(const char* path, mbe_graph** out);
 
 /* Builds a graph from a host CSR in file orientation.  Lists may be
@@ -166,6 +167,20 @@ MBE_API mbe_status mbe_graph_generate(const mbe_gen_params* params, mbe_graph** 
 
 /* Writes the `.bi` layout data/gen_bi.cpp:72-79 writes. */
 MBE_API mbe_status mbe_graph_write_bi(const mbe_graph* g, const char* path);
+
+/* Binary graph image: the normalised CSR (row_ptr, col_idx) behind a
+ * checksummed header, loaded without parsing or normalising.  No reference
+ * counterpart: the reference re-parses its text file on every run
+ * (src/main.cu:38-48).  Loading verifies the checksum, the sizes and the
+ * CSR invariants (monotone offsets, sorted unique ids in range) and
+ * returns MBE_ERR_FORMAT otherwise. */
+MBE_API mbe_status mbe_graph_write_bin(const mbe_graph* g, const char* path);
+MBE_API mbe_status mbe_graph_load_bin(const char* path, mbe_graph** out);
+
+/* Loads the `.bi` file bi_path through a binary cache at cache_path: the
+ * cache is used when it is at least as new as bi_path and intact;
+ * otherwise bi_path is parsed and the cache (re)written, best effort. */
+MBE_API mbe_status mbe_graph_load_cached(const char* bi_path, const char* cache_path, mbe_graph** out);
 
 MBE_API mbe_status mbe_graph_info_get(const mbe_graph* g, mbe_graph_info* out);
 

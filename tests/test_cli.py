@@ -67,3 +67,15 @@ def test_cli_emit_file(built, tmp_path):
         n += 1
     assert n == exp["count"] == len(seen)
     assert f"0x{h:016x}" == exp["hash"]
+
+
+@pytest.mark.gpu
+def test_cli_takes_a_binary_image(built, tmp_path):
+    exp = json.load(open(os.path.join(GOLD, "expected.json")))["power_law_2k_1k"]
+    img = tmp_path / "power_law_2k_1k.mbeg"
+    cm.Graph.load_bi(os.path.join(GOLD, exp["file"])).write_bin(str(img))
+    r = subprocess.run([cm.CLI_PATH, str(img)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[5] == f"maximal bicliques: {exp['count']}"
+    assert lines[7] == f"hash: {exp['hash']}"
