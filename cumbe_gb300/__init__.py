@@ -90,6 +90,7 @@ SIGNATURES = {
     "mbe_graph_write_bin": (ctypes.c_int, [_VP, ctypes.c_char_p]),
     "mbe_graph_load_bin": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
     "mbe_graph_load_cached": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "mbe_graph_load_konect": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
     "mbe_graph_info_get": (ctypes.c_int, [_VP, ctypes.POINTER(_GraphInfo)]),
     "mbe_graph_copy_csr": (ctypes.c_int, [_VP, _U64P, _U32P]),
     "mbe_graph_free": (None, [_VP]),
@@ -225,6 +226,14 @@ class Graph:
     def load_bin(cls, path: str) -> "Graph":
         h = _VP()
         _check(lib().mbe_graph_load_bin(os.fsencode(path), ctypes.byref(h)), "mbe_graph_load_bin")
+        return cls(h)
+
+    @classmethod
+    def load_konect(cls, path: str, skip_words: int = 0, skip_per_edge: int = 0) -> "Graph":
+        """KONECT edge-pair file, numbered as data/gen_bi.cpp numbers it."""
+        h = _VP()
+        _check(lib().mbe_graph_load_konect(os.fsencode(path), skip_words, skip_per_edge, ctypes.byref(h)),
+               "mbe_graph_load_konect")
         return cls(h)
 
     @classmethod

@@ -18,6 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmbe.so")
 CLI = os.path.join(HERE, "mbe")
+GEN_BI = os.path.join(HERE, "gen_bi")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["graph_host.cpp", "graph_dev.cu", "engine.cu", "capi.cu", "capi_static.cu", "server.cu"]
@@ -90,6 +91,11 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         subprocess.check_call(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), cli_src,
                                "-o", CLI + ".tmp", "-L" + HERE, "-lmbe", "-Wl,-rpath,$ORIGIN"])
         os.replace(CLI + ".tmp", CLI)
+    gen_src = os.path.join(CSRC, "gen_bi_cli.cpp")
+    if force or _stale(GEN_BI, [gen_src, LIB]):
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), gen_src,
+                               "-o", GEN_BI + ".tmp", "-L" + HERE, "-lmbe", "-Wl,-rpath,$ORIGIN"])
+        os.replace(GEN_BI + ".tmp", GEN_BI)
     return LIB
 
 

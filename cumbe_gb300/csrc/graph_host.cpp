@@ -12,6 +12,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "mbe_hash.h"
@@ -456,6 +457,71 @@ extern "C" mbe_status mbe_graph_load_cached(const char* bi_path, const char* cac
     if (st != MBE_OK) return st;
     mbe_graph_write_bin(*out, cache_path);  // best effort: the graph is loaded either way
     clear_error();
+    return MBE_OK;
+}
+
+// KONECT edge-pair text -> bipartite graph, as data/gen_bi.cpp builds it:
+// skip `skip_words` leading tokens, then read "source target" pairs each
+// followed by `skip_per_edge` ignored tokens until the text ends or a pair
+// does not parse as integers; rows are sources and cols targets, each
+// numbered by first appearance; repeated pairs count once.
+extern "C" mbe_status mbe_graph_load_konect(const char* path, uint32_t skip_words, uint32_t skip_per_edge,
+                                            mbe_graph** out) {
+    clear_error();
+    if (!path || !out) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    std::vector<char> buf;
+    mbe_status st = read_file(path, buf);
+    if (st != MBE_OK) return st;
+    const char* c = buf.data();
+    const char* end = c + buf.size();
+    auto token = [&](const char** b, const char** e) -> bool {
+        while (c < end && is_ws(*c)) c++;
+        if (c >= end) return false;
+        *b = c;
+        while (c < end && !is_ws(*c)) c++;
+        *e = c;
+        return true;
+    };
+    // an int32 like `istream >> int`: optional sign, digits, no overflow
+    auto as_int = [](const char* b, const char* e, int* v) -> bool {
+        long long x;
+        if (!parse_token(b, e, &x) || x < INT32_MIN || x > INT32_MAX) return false;
+        *v = (int)x;
+        return true;
+    };
+    const char *b, *e;
+    for (uint32_t i = 0; i < skip_words; i++)
+        if (!token(&b, &e)) break;
+    std::unordered_map<int, uint32_t> rid, cid;
+    std::vector<std::pair<uint32_t, uint32_t>> pairs;
+    for (;;) {
+        int r, l;
+        if (!token(&b, &e) || !as_int(b, e, &r)) break;
+        if (!token(&b, &e) || !as_int(b, e, &l)) break;
+        for (uint32_t i = 0; i < skip_per_edge; i++)
+            if (!token(&b, &e)) break;
+        auto ir = rid.emplace(r, (uint32_t)rid.size()).first->second;
+        auto il = cid.emplace(l, (uint32_t)cid.size()).first->second;
+        pairs.emplace_back(ir, il);
+    }
+    auto* g = new (std::nothrow) mbe_graph();
+    if (!g) return fail(MBE_ERR_OUT_OF_MEMORY, "host allocation failed");
+    g->n_rows = (uint32_t)rid.size();
+    g->n_cols = (uint32_t)cid.size();
+    g->row_ptr.assign((size_t)g->n_rows + 1, 0);
+    for (auto& pr : pairs) g->row_ptr[pr.first + 1]++;
+    for (uint32_t r = 0; r < g->n_rows; r++) g->row_ptr[r + 1] += g->row_ptr[r];
+    g->col_idx.resize(pairs.size());
+    std::vector<uint64_t> fill(g->row_ptr.begin(), g->row_ptr.end() - 1);
+    for (auto& pr : pairs) g->col_idx[fill[pr.first]++] = pr.second;
+    st = normalise(g);
+    if (st != MBE_OK) {
+        delete g;
+        return st;
+    }
+    g->uid = next_graph_uid();
+    *out = g;
     return MBE_OK;
 }
 

@@ -182,6 +182,16 @@ MBE_API mbe_status mbe_graph_load_bin(const char* path, mbe_graph** out);
  * otherwise bi_path is parsed and the cache (re)written, best effort. */
 MBE_API mbe_status mbe_graph_load_cached(const char* bi_path, const char* cache_path, mbe_graph** out);
 
+/* Builds a graph from a KONECT edge-pair file the way data/gen_bi.cpp:14-60
+ * does: skip_words leading tokens are skipped (the "%" header lines), then
+ * "source target" pairs are read, each followed by skip_per_edge ignored
+ * tokens (weights, timestamps), until the text ends or a pair is not two
+ * integers.  Rows are sources, cols targets, each numbered by first
+ * appearance; repeated pairs count once.  mbe_graph_write_bi then writes
+ * the same `.bi` graph gen_bi writes (row lists sorted here). */
+MBE_API mbe_status mbe_graph_load_konect(const char* path, uint32_t skip_words, uint32_t skip_per_edge,
+                                         mbe_graph** out);
+
 MBE_API mbe_status mbe_graph_info_get(const mbe_graph* g, mbe_graph_info* out);
 
 /* Copies the normalised CSR out: row_ptr[n_rows+1], col_idx[n_edges]. */

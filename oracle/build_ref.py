@@ -11,6 +11,8 @@ Test infrastructure (the oracle's pin).  Outputs go to oracle/_ref/ only
                    present; elsewhere a previously built cubin is used.
   ref_runner       oracle/ref_runner.cpp (host side, CUDA driver API),
                    built wherever CUDA headers are present.
+  gen_bi           the reference's KONECT converter data/gen_bi.cpp,
+                   compiled unmodified with g++ (reference sources only).
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ OUT = os.path.join(HERE, "_ref")
 REF_ROOT = "/root/reference"
 CUBIN = os.path.join(OUT, "cumbe_ref.cubin")
 RUNNER = os.path.join(OUT, "ref_runner")
+GEN_BI = os.path.join(OUT, "gen_bi")
 
 
 def _cuda_home() -> str:
@@ -42,6 +45,11 @@ def build() -> dict:
                             "-o", CUBIN], check=True, capture_output=True)
     if os.path.exists(CUBIN):
         out["cubin"] = CUBIN
+    # the reference's KONECT converter, from its own unmodified source
+    gen_src = os.path.join(REF_ROOT, "data", "gen_bi.cpp")
+    if os.path.exists(gen_src) and not os.path.exists(GEN_BI):
+        subprocess.run(["g++", "-O3", "-std=c++17", gen_src, "-o", GEN_BI], check=True, capture_output=True)
+    out["gen_bi"] = GEN_BI if os.path.exists(GEN_BI) else None
     runner_src = os.path.join(HERE, "ref_runner.cpp")
     inc = os.path.join(cuda, "include")
     if os.path.exists(os.path.join(inc, "cuda.h")):
