@@ -160,6 +160,11 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
                 if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
         EngineConfig cfg = make_config(variant, opts, sw);
         cfg.emit = emit;
+        // Many graphs: chunks of ~128 MiB of root records, so that the DFS
+        // reads each chunk's records while they are still in L2 (measured:
+        // 4,096 mixed graphs 19.4 s -> 17.2 s).  One graph keeps one chunk:
+        // every chunk ends in a load-imbalance tail, which costs more there.
+        if (n > 1 && !cfg.pool_words) cfg.chunk_words = 32ull << 20;
         std::vector<ResultAcc> part;
         EngineStats ps;
         mbe_status st = engine_run(eb, s, cfg, devs, split ? sel : roots, part, &ps, io);

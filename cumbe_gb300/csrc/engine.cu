@@ -2171,7 +2171,13 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         if (const char* env = std::getenv("MBE_ARENA_WORDS")) want = std::strtoull(env, nullptr, 10);
         eb.arena_words = (uint32_t)std::max<uint64_t>(std::min(want, cap), 1u << 14) & ~31u;
     }
-    if (!eb.pool_words) eb.pool_words = 1ull << 31;
+    if (!eb.pool_words) {
+        eb.pool_words = 1ull << 31;
+        if (const char* e = std::getenv("MBE_POOL_INIT_MB")) {  // tuning: first pool size
+            const unsigned long long mb = std::strtoull(e, nullptr, 10);
+            if (mb) eb.pool_words = mb * (1ull << 20) / 4;
+        }
+    }
     const uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
     const uint32_t retry_cap = 1u << 16;
 
@@ -2280,7 +2286,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         }
         a.pool = (uint32_t*)eb.pool.ptr;
         a.pool_words = pool_words;
-        a.pool_watermark = pool_words / 2;
+        a.pool_watermark = cfg.chunk_words ? std::min<uint64_t>(cfg.chunk_words, pool_words / 2) : pool_words / 2;
         MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));  // kernels restore -1 after each root
         MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
         if (cfg.emit) MBE_CUDA_TRY(cudaMemsetAsync(cfg.emit->ctl, 0, 3 * sizeof(unsigned long long), s));
@@ -2469,6 +2475,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         stats->grid_a = gridA;
         stats->grid_b = gridB;
     }
+    if (std::getenv("MBE_VERBOSE"))
+        std::fprintf(stderr, "engine: %u graphs, %zu roots, %u chunks, pool %.1f GiB, expand %.2f ms, dfs %.2f ms\n",
+                     ng, roots.size(), chunks, eb.pool_words * 4.0 / (1u << 30), ms_a, ms_b);
     return MBE_OK;
 }
 

@@ -48,6 +48,7 @@ struct EngineConfig {
     uint32_t max_frames = 512;
     uint32_t arena_words = 0;           // per warp; 0 = engine default
     uint64_t pool_words = 0;            // node pool cap; 0 = engine default (grows on demand)
+    uint64_t chunk_words = 0;           // root records per chunk; 0 = half the pool
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
     unsigned long long timeout_ns = 60ull * 1000000000ull;
     const EmitTarget* emit = nullptr;
