@@ -115,3 +115,17 @@ def test_donation_granularity_does_not_change_results(engine):
     for dm in (2, 3, 8, 64):
         got = engine.enumerate(G, "cuMBE", donate_min=dm)
         assert (got.count, got.hash) == (base.count, base.hash), dm
+
+
+def test_stress_graph_shape_small_scale(engine):
+    """The load-imbalance stress graph's shape (Chung-Lu gamma 1.9 on both
+    sides, no degree cap, a planted K_{20,30} block at density 0.9 over hubs)
+    at 1/250 of its size: 5,600 x 2,000, 32,000 edges, 920,386 bicliques."""
+    G = cm.Graph.generate(5600, 2000, 32000, 1.9, 1.9, 0, 3, planted=1, planted_rows=20, planted_cols=30,
+                          planted_density=0.9)
+    nr, nc, rp, ci = G.csr()
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=os.cpu_count() or 8)
+    assert want.count == 920386
+    for v in ("cuMBE", "noWS"):
+        got = engine.enumerate(G, v)
+        assert (got.count, got.hash) == (want.count, want.hash), v
