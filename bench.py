@@ -70,17 +70,22 @@ def peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic(workload):
-    """Per-launch DRAM bytes of dfs_kernel from the committed ncu summary
-    (profiles/dfs_kernel_<workload>.md, line 'traffic_bytes_per_launch: N')."""
+def profile_value(workload, key):
+    """A figure of dfs_kernel from the committed ncu summary
+    (profiles/dfs_kernel_<workload>.md, a line '<key>: N')."""
     p = os.path.join(ROOT, "profiles", f"dfs_kernel_{workload}.md")
     try:
         for line in open(p):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def profile_traffic(workload):
+    """Per-launch DRAM bytes of dfs_kernel (line 'traffic_bytes_per_launch: N')."""
+    return profile_value(workload, "traffic_bytes_per_launch")
 
 
 class ClockSampler:
@@ -226,6 +231,22 @@ def served_leg(rate=2000.0, n_requests=4000, seed=11):
             "pool": "the 2,000 x 1,000 power-law graph + the batch graphs with |U| <= 1000"}
 
 
+def stress_leg(eng):
+    """The load-imbalance stress graph's shape (Chung-Lu gamma 1.9 on both
+    sides, uncapped, planted K_{20,30} blocks at density 0.9 over hubs) at
+    1/50 of its size: its full size has far more maximal bicliques than any
+    engine can enumerate (the count grows ~40x per doubling of the graph)."""
+    import cumbe_gb300 as cm
+    p = dict(n_rows=28000, n_cols=10000, n_edges=160000, gamma_rows=1.9, gamma_cols=1.9, max_deg=0, seed=3,
+             planted=4, planted_rows=20, planted_cols=30, planted_density=0.9)
+    g = cm.Graph.generate(**p)
+    eng.enumerate(cm.Graph.generate(**dict(p, n_rows=14000, n_cols=5000, n_edges=80000, planted=2)))  # warm-up
+    r = eng.enumerate(g)
+    eng.release(g)
+    return {"workload": "stress shape at 1/50 scale", **p, "bicliques": r.count, "hash": f"{r.hash:#018x}",
+            "ms": r.ms, "bicliques_per_s": r.count / (r.ms / 1e3)}
+
+
 def run_reference(args, wl, rank, world):
     """--impl reference: the CPU restatement of the reference's search."""
     if rank != 0:
@@ -268,6 +289,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-stress", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -349,7 +371,10 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind, "kernel": "dfs_kernel",
                 "algorithmic_bytes_per_launch": tot_words * 4 // args.steps,
-                "launch_ms": tot_dfs_ms / args.steps}
+                "launch_ms": tot_dfs_ms / args.steps,
+                # from the committed ncu summaries: the kernel is L1/L2- and latency-bound
+                "l2_hit_rate": profile_value(args.workload, "l2_hit_rate"),
+                "int_pipe_active": profile_value(args.workload, "int_pipe_active")}
 
     line = {"metric": "maximal bicliques/sec", "value": value, "unit": "bicliques/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -368,6 +393,8 @@ def main():
         line["served"] = served_leg()
         # saturating load: arrivals faster than one request per launch can serve
         line["served_saturated"] = served_leg(rate=20000.0, n_requests=20000, seed=12)
+    if rank == 0 and not args.no_stress:
+        line["stress"] = stress_leg(eng)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rc, dt, stride = cpu_baseline(g, wl, threads)
