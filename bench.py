@@ -181,7 +181,7 @@ def batched_leg(eng, n_graphs=4096):
 
 def served_leg(rate=2000.0, n_requests=4000, seed=11):
     """Poisson request stream against a device-resident pool: continuous
-    batching (2 slots on half the GPU each, up to 256 requests per launch)
+    batching (2 slots of 2 DFS blocks per SM each, up to 256 requests per launch)
     vs one request per launch on the whole GPU.  Half the requests are
     thresholded (|A| >= a, |B| >= b, a, b uniform in 1..5)."""
     import numpy as np
@@ -222,7 +222,7 @@ def served_leg(rate=2000.0, n_requests=4000, seed=11):
                 "requests_per_s": n_requests / span, "bicliques_per_s": tot / span, "all_ok": ok,
                 "mean_batch": float(np.mean([r["batch_size"] for r in out]))}, res
 
-    cont, r1 = run(2, 256, 1)
+    cont, r1 = run(2, 256, 2)
     plain, r2 = run(1, 1, 0)
     same = [r1[k] for k in sorted(r1)] == [r2[k] for k in sorted(r2)]
     return {"rate_req_per_s": rate, "requests": n_requests, "pool_graphs": len(pool),

@@ -356,7 +356,7 @@ class Server:
     (mbe_server_*).  Requests are answered asynchronously; poll() returns
     finished ones with their timestamps on the server clock."""
 
-    def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 1,
+    def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 2,
                  variant: str = "cuMBE", mem_budget: int = 0):
         cfg = _ServerConfig(slots, max_batch, blocks_per_sm, VARIANTS[variant], mem_budget)
         self._h = _VP()

@@ -37,11 +37,14 @@ def _flags() -> list[str]:
     if os.environ.get("MBE_PROFILE") == "1":
         f += ["-DMBE_PROFILE"]
     # MBE_DFS_BLOCKS=N sets the resident blocks per SM the enumeration kernel
-    # is compiled for (its register budget); default 2.
+    # is compiled for (its register budget); default 5.
     if os.environ.get("MBE_DFS_BLOCKS"):
         f += ["-DMBE_DFS_MIN_BLOCKS=%d" % int(os.environ["MBE_DFS_BLOCKS"])]
     # MBE_UNROLL=E,G,P sets the scan unroll factors of the enumeration kernel
     # (expansion chunks, gather chunks, prefilter rows); default 1,1,8.
+    # MBE_DFS_WARPS=N sets its warps per block; default 4.
+    if os.environ.get("MBE_DFS_WARPS"):
+        f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]
     if os.environ.get("MBE_EVAL_NOINLINE") == "1":
         f += ["-DMBE_EVAL_NOINLINE"]
     if os.environ.get("MBE_UNROLL"):

@@ -38,8 +38,8 @@ namespace {
 constexpr size_t kStaticScratchBytes = (size_t)MBE_STATIC_SCRATCH_BYTES;
 constexpr uint32_t kStaticMaxVertices = MBE_STATIC_MAX_VERTICES;
 constexpr uint32_t kGridA = 32;          // root-expansion blocks
-constexpr uint32_t kGridB = 16;          // DFS blocks of 8 warps
-constexpr uint32_t kWarps = kGridB * 8;
+constexpr uint32_t kWarps = 128;                   // DFS warps
+constexpr uint32_t kGridB = kWarps / kDfsWarps;    // DFS blocks
 constexpr uint32_t kArenaWords = 16384;  // 64 KiB DFS arena per warp
 constexpr uint32_t kMaxFrames = 256;
 constexpr uint32_t kRetryCap = 1024;

@@ -32,7 +32,7 @@ namespace mbe {
 namespace {
 
 constexpr int kThreadsA = 256;
-constexpr int kWarpsB = 8;
+constexpr int kWarpsB = kDfsWarps;
 constexpr int kThreadsB = kWarpsB * 32;
 constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
@@ -1823,9 +1823,6 @@ __device__ void prof_idle(const EngineArgs& a, unsigned long long t0, unsigned l
 }
 #endif
 
-#ifndef MBE_DFS_MIN_BLOCKS
-#define MBE_DFS_MIN_BLOCKS 2  // 16 warps per SM with a 128-register budget: no spills
-#endif
 __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(EngineArgs a) {
     __shared__ uint32_t sLi[kWarpsB][kSmemW];
     __shared__ uint32_t sNz[kWarpsB][kSmemW];

@@ -25,6 +25,18 @@
 
 namespace mbe {
 
+// Shape of the DFS kernel: warps per block and the resident blocks per SM
+// it is compiled for (the register budget).  4 x 5 = 20 warps per SM at 96
+// registers measured fastest (8 x 2 at 128 registers: +3%; 8 x 3 at 80 with
+// spills: +6%).
+#ifndef MBE_DFS_WARPS
+#define MBE_DFS_WARPS 4
+#endif
+#ifndef MBE_DFS_MIN_BLOCKS
+#define MBE_DFS_MIN_BLOCKS 5
+#endif
+constexpr int kDfsWarps = MBE_DFS_WARPS;
+
 constexpr uint32_t kHdrWords = 16;
 constexpr uint32_t kMaxPath = 27;
 

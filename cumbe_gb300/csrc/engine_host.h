@@ -71,7 +71,7 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
                     const EmitTarget* emit = nullptr);
 
 // Raw launchers of the two enumeration kernels (256 threads per block;
-// dfs_kernel runs 8 warps per block).
+// dfs_kernel runs kDfsWarps warps per block).
 cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s);
 cudaError_t launch_dfs(const EngineArgs& a, unsigned grid, cudaStream_t s);
 

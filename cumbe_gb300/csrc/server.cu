@@ -192,7 +192,7 @@ extern "C" mbe_status mbe_server_start(int device, const mbe_server_config* cfg,
     if (!s->cfg.slots) s->cfg.slots = 2;
     if (!s->cfg.max_batch) s->cfg.max_batch = 256;
     if (!s->cfg.mem_budget) s->cfg.mem_budget = 120ull << 30;
-    if (!cfg) s->cfg.blocks_per_sm = 1;
+    if (!cfg) s->cfg.blocks_per_sm = 2;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {

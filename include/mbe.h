@@ -260,7 +260,7 @@ typedef struct mbe_server mbe_server;
 typedef struct mbe_server_config {
     uint32_t slots;              /* default 2                               */
     uint32_t max_batch;          /* default 256 (1 = one request per launch) */
-    uint32_t blocks_per_sm;      /* default 1; 0 = the whole GPU per slot   */
+    uint32_t blocks_per_sm;      /* default 2; 0 = the whole GPU per slot   */
     uint32_t variant;            /* mbe_variant                             */
     uint64_t mem_budget;         /* default 120 GB                          */
 } mbe_server_config;
