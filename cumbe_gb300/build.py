@@ -45,6 +45,9 @@ def _flags() -> list[str]:
     # MBE_DFS_WARPS=N sets its warps per block; default 4.
     if os.environ.get("MBE_DFS_WARPS"):
         f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]
+    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX"):  # tuning sweeps
+        if os.environ.get(knob):
+            f += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if os.environ.get("MBE_EVAL_NOINLINE") == "1":
         f += ["-DMBE_EVAL_NOINLINE"]
     if os.environ.get("MBE_UNROLL"):

@@ -36,7 +36,14 @@ constexpr int kWarpsB = kDfsWarps;
 constexpr int kThreadsB = kWarpsB * 32;
 constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
-constexpr uint32_t kKeepWindow = 32;     // Q rows a dropped Q row is tested against
+#ifndef MBE_KEEP_WINDOW
+#define MBE_KEEP_WINDOW 32
+#endif
+#ifndef MBE_POP_SLEEP_MAX
+#define MBE_POP_SLEEP_MAX 1024
+#endif
+constexpr uint32_t kKeepWindow = MBE_KEEP_WINDOW;  // Q rows a dropped Q row is tested against (<= 32)
+constexpr unsigned kPopSleepMax = MBE_POP_SLEEP_MAX;  // ns, back-off ceiling of a warp waiting for a task
 constexpr uint32_t kShRows = 128;        // Q' rows / P' keys of a packed build kept in shared memory
 #ifndef MBE_UNROLL_E
 #define MBE_UNROLL_E 1
@@ -795,7 +802,7 @@ __device__ __noinline__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my
                 break;
             }
             __nanosleep(sleep_ns);
-            if (sleep_ns < 1024) sleep_ns <<= 1;
+            if (sleep_ns < kPopSleepMax) sleep_ns <<= 1;
             unsigned long long now = globaltimer_ns();
             unsigned long long prog = ld_volatile(a.progress);
             if (prog != last_prog) {
