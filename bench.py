@@ -61,6 +61,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest of the ranks' values of x (the slowest replica's step
+    time); x itself on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(count_per_step, world, ms_per_step):
+    """Whole-job bicliques/s of `world` replicas that each enumerate
+    count_per_step bicliques per step, timed by the slowest replica."""
+    return count_per_step * world / (ms_per_step / 1000.0)
+
+
 def peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -341,12 +359,8 @@ def main():
     c1 = eng.counters()
     if any((x.count, x.hash) != (r0.count, r0.hash) for x in results):
         raise SystemExit("enumeration results differ between steps")
-    ms_step = tot_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = tot_count * world / (ms_step * args.steps / 1000.0)
+    ms_step = max_over_ranks(tot_ms / args.steps, world, f"cuda:{local}")
+    value = replicas_value(tot_count / args.steps, world, ms_step)
 
     # ---- end to end through the C ABI from host buffers (e2e) ----
     e_c0 = eng.counters()

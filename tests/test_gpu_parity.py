@@ -129,3 +129,27 @@ def test_stress_graph_shape_small_scale(engine):
     for v in ("cuMBE", "noWS"):
         got = engine.enumerate(G, v)
         assert (got.count, got.hash) == (want.count, want.hash), v
+
+
+@pytest.mark.parametrize("env", [{"MBE_SOLVE_ROWS": "0"}, {"MBE_SOLVE_ROWS": "16"}, {"MBE_DONATE_COPY": "0"},
+                                 {"MBE_SOLVE_ROWS": "0", "MBE_DONATE_COPY": "0"}])
+def test_alternative_paths_give_the_same_bicliques(engine, env):
+    """The record path instead of the register search, and path-replay
+    donation instead of pool copies, must not change any result."""
+    G = cm.Graph.generate(3000, 1500, 16000, 2.0, 2.2, 0, 4)
+    rng = np.random.default_rng(8)
+    H = cm.Graph.from_csr(*random_csr(rng, 90, 60, 0.15))
+    base = [engine.enumerate(x) for x in (G, H)]
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        got = [engine.enumerate(x) for x in (G, H)]
+        em = engine.enumerate(H, emit_cap=base[1].count)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+    assert [(r.count, r.hash) for r in got] == [(r.count, r.hash) for r in base], env
+    assert (em.count, em.hash, len(em.bicliques)) == (base[1].count, base[1].hash, base[1].count)
