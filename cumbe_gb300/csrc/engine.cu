@@ -375,34 +375,30 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
         const uint32_t* L0 = G.r_adj + G.r_ptr[x];
         const uint32_t W = (d + 31) / 32;
 
-        // 1. candidates C = N(N(x)) \ {x}: first toucher claims a slot
+        // 1. candidates C = N(N(x)) \ {x}: first toucher claims a slot.  With
+        // the reverse scan the same scatter also counts |N(v) n L0|
+        // (src/mbe_cuMBE.cuh:215-227): the per-block map holds touches - 1.
         unsigned long long scan = 0;
         for (uint32_t j = warp; j < d; j += nwarps) {
             uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
             scan += e - b;
             for (uint32_t k = b + lane; k < e; k += 32) {
                 uint32_t v = G.l_adj[k];
-                if (v != x && atomicCAS(&cmap[v], -1, -2) == -1) cl[atomicAdd(&s_ncand, 1u)] = v;
+                if (v == x) continue;
+                const int old = rs ? atomicAdd(&cmap[v], 1) : atomicCAS(&cmap[v], -1, -2);
+                if (old == -1) cl[atomicAdd(&s_ncand, 1u)] = v;
             }
         }
         __syncthreads();
         const uint32_t n = s_ncand;
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            cmap[cl[i]] = (int)i;
-            cntA[i] = 0;
+            const uint32_t v = cl[i];
+            cntA[i] = rs ? (uint32_t)(cmap[v] + 1) : 0u;
+            cmap[v] = (int)i;
         }
         __syncthreads();
-        // 2. |N(v) n L0| per candidate
-        if (rs) {
-            // reverse scan: scatter from every u in L0 (src/mbe_cuMBE.cuh:215-227)
-            for (uint32_t j = warp; j < d; j += nwarps) {
-                uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
-                for (uint32_t k = b + lane; k < e; k += 32) {
-                    uint32_t v = G.l_adj[k];
-                    if (v != x) atomicAdd(&cntA[cmap[v]], 1u);
-                }
-            }
-        } else {
+        // 2. |N(v) n L0| per candidate (already counted by the reverse scan)
+        if (!rs) {
             // forward scan: each candidate's own list against sorted L0
             // (src/mbe_noRS.cuh:274-283)
             for (uint32_t i = warp; i < n; i += nwarps) {
@@ -483,7 +479,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
             }
             if (ok) {
                 ResultAcc* r = &a.results[rt.x];
-                unsigned long long words = s_scan * (rs ? 3 : 2) + d;
+                unsigned long long words = s_scan * 2 + d;
                 atomicAdd(&r->nodes, 1ull);
                 atomicAdd(&r->words_expand, words);
                 if (!s_nonmax && nRset >= a.minR) {
