@@ -759,6 +759,7 @@ struct WarpCtx {
     uint32_t* sNz;
     uint32_t* scrPack;     // 2 x kc words: srow, spos of a packed build too large for shared memory
     uint32_t* scrAbs;      // scr_n words: ranks absorbed by the child being evaluated (output stream only)
+    uint32_t scr_kc;       // key-array capacity of this launch's scratch layout
     uint32_t* sBucket;     // 64 words of shared memory: Q' then P' count buckets
     uint32_t* shRow;       // kShRows Q' rows of a packed build (shared memory)
     uint32_t* shPos;       // their parent positions
@@ -1061,7 +1062,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     const uint32_t m = bucket_offsets(sb);
     const bool shq = m <= kShRows;
     uint32_t* srow = shq ? wc.shRow : wc.scrPack;
-    uint32_t* spos = shq ? wc.shPos : wc.scrPack + a.scr_kc;
+    uint32_t* spos = shq ? wc.shPos : wc.scrPack + wc.scr_kc;
     for (uint32_t base = 0; base < xi; base += 32 * kUnrollG) {
         uint32_t r[kUnrollG];
 #pragma unroll
@@ -1840,16 +1841,28 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
     WarpCtx wc;
     wc.arena = a.arena + gw * a.arena_words;
     wc.arena_top = 0;
-    uint32_t* scr = a.scratch + gw * a.scratch_words;
-    // scratch: Li[max_W] Nz[max_W] qcnt[scr_n] | keysP[kc] keysQ[kc] (u64, kc = pow2 >= scr_n)
+    // scratch layout: Li[max_W] Nz[max_W] qcnt[scr_n] | keysP[kc] keysQ[kc]
+    // (u64) | srow/spos[2 kc] | absorbed[scr_n] (output stream), kc = the
+    // power of two >= scr_n; scr_n from the largest root record of the chunk
+    uint32_t scr_n = a.scr_n, kc = a.scr_kc;
+    size_t sw = a.scratch_words;
+    if (a.scratch_dyn) {
+        scr_n = max(*(const volatile uint32_t*)a.max_n, 32u);
+        kc = 32;
+        while (kc < scr_n) kc <<= 1;
+        sw = ((((2 * (size_t)a.max_W + scr_n + 1) & ~(size_t)1) + 6 * (size_t)kc + (a.emit ? scr_n : 0)) + 31) &
+             ~(size_t)31;
+    }
+    uint32_t* scr = a.scratch + gw * sw;
     wc.scrLi = scr;
     wc.scrNz = scr + a.max_W;
     wc.scrQcnt = scr + 2 * (size_t)a.max_W;
-    size_t koff = (2 * (size_t)a.max_W + a.scr_n + 1) & ~(size_t)1;
+    size_t koff = (2 * (size_t)a.max_W + scr_n + 1) & ~(size_t)1;
     wc.scrKeysP = (unsigned long long*)(scr + koff);
-    wc.scrKeysQ = wc.scrKeysP + a.scr_kc;
-    wc.scrPack = (uint32_t*)(wc.scrKeysQ + a.scr_kc);
-    wc.scrAbs = wc.scrPack + 2 * (size_t)a.scr_kc;
+    wc.scrKeysQ = wc.scrKeysP + kc;
+    wc.scrPack = (uint32_t*)(wc.scrKeysQ + kc);
+    wc.scrAbs = wc.scrPack + 2 * (size_t)kc;
+    wc.scr_kc = kc;
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
     wc.sBucket = sBucket[warp];
@@ -2126,6 +2139,12 @@ struct Ctrl {
 };
 }  // namespace
 
+// Words of one warp's DFS scratch for records of up to scr_n candidates
+// (kc = the power of two >= scr_n); the DFS kernel lays it out the same way.
+static size_t scratch_layout_words(uint32_t maxW, uint32_t scr_n, size_t kc, bool emit) {
+    return align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 6 * kc + (emit ? scr_n : 0), 32);
+}
+
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
                       const std::vector<const DeviceGraph*>& gs, const std::vector<uint2>& roots,
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io) {
@@ -2269,6 +2288,19 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.prof_a = prof_dev + prof_n - 16;
 #endif
 
+    {
+        // No readback between the kernels when the scratch can be sized for
+        // the bound on any record (fewer than |R| candidates) within 4 GiB.
+        const uint32_t scr_b = std::max<uint32_t>(maxNR, 32);
+        size_t kc = 32;
+        while (kc < scr_b) kc <<= 1;
+        const size_t bytes = sizeof(uint32_t) * (size_t)nwarpsB * scratch_layout_words(maxW, scr_b, kc, cfg.emit != nullptr);
+        if (bytes <= (4ull << 30)) {
+            if ((st = eb.scratch.ensure(bytes))) return st;
+            a.scratch = (uint32_t*)eb.scratch.ptr;
+            a.scratch_dyn = 1;
+        }
+    }
     cudaEvent_t e0, e1, e2;
     MBE_CUDA_TRY(cudaEventCreate(&e0));
     MBE_CUDA_TRY(cudaEventCreate(&e1));
@@ -2323,17 +2355,18 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
             MBE_CUDA_TRY(cudaGetLastError());
             MBE_CUDA_TRY(cudaEventRecord(e1, s));
-            // DFS scratch is laid out for the largest record this chunk made
-            uint32_t max_n = 0;
-            MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
-            MBE_CUDA_TRY(cudaStreamSynchronize(s));
-            io->d2h += sizeof max_n;
-            {
+            // DFS scratch is laid out for the largest record this chunk made:
+            // by the kernel itself when the scratch is sized for the bound,
+            // else from a readback of that size
+            if (!a.scratch_dyn) {
+                uint32_t max_n = 0;
+                MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
+                MBE_CUDA_TRY(cudaStreamSynchronize(s));
+                io->d2h += sizeof max_n;
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
                 while (kc < scr_n) kc <<= 1;
-                size_t sw = align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 4 * kc + 2 * kc +
-                                         (cfg.emit ? scr_n : 0), 32);
+                size_t sw = scratch_layout_words(maxW, scr_n, kc, cfg.emit != nullptr);
                 if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
                 a.scratch = (uint32_t*)eb.scratch.ptr;
                 a.scratch_words = (uint32_t)sw;

@@ -195,6 +195,8 @@ struct EngineArgs {
     uint32_t scratch_words;
     uint32_t scr_n;            // candidate bound the scratch is laid out for
     uint32_t scr_kc;           // key-array capacity (power of two >= scr_n)
+    uint32_t scratch_dyn;      // 1: the DFS kernel lays its scratch out from *max_n itself
+                               //    (scratch sized for the bound; scr_n / scr_kc / scratch_words unused)
     uint32_t max_W;            // largest universe word count
     // section cycle counters (builds with -DMBE_PROFILE only; else null)
     unsigned long long* prof;  // [kProfSlots + warps + 2 * kProfBins]
