@@ -2150,6 +2150,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io) {
     const uint32_t ng = (uint32_t)gs.size();
     results.assign(ng, ResultAcc{});
+    // the per-graph results are read with each chunk's control block when
+    // they are small (the last chunk's copy is the final one)
+    const bool results_with_ctrl = sizeof(ResultAcc) * ng <= 4096;
     if (ng == 0 || roots.empty()) return MBE_OK;
     uint32_t maxNR = 1, maxW = 1, maxRD = 1;
     for (const DeviceGraph* g : gs) {
@@ -2379,6 +2382,11 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             io->launches += 2;
             Ctrl hc;
             MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            if (results_with_ctrl) {  // small result sets ride along: one synchronisation per chunk
+                MBE_CUDA_TRY(cudaMemcpyAsync(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng,
+                                             cudaMemcpyDeviceToHost, s));
+                io->d2h += sizeof(ResultAcc) * ng;
+            }
             MBE_CUDA_TRY(cudaStreamSynchronize(s));
             io->d2h += sizeof(Ctrl);
             float t1 = 0, t2 = 0;
@@ -2440,8 +2448,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
     if (result != MBE_OK) return result;
-    MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
-    io->d2h += sizeof(ResultAcc) * ng;
+    if (!results_with_ctrl) {
+        MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
+        io->d2h += sizeof(ResultAcc) * ng;
+    }
 #ifdef MBE_PROFILE
     {
         unsigned long long hp[kProfSlots];
