@@ -315,6 +315,6 @@ extern "C" mbe_status mbe_ctx_last_grid(mbe_ctx* ctx, uint32_t* grid_expand, uin
     if (!ctx) return fail(MBE_ERR_INVALID_ARG, "null argument");
     if (grid_expand) *grid_expand = ctx->last_stats.grid_a;
     if (grid_dfs) *grid_dfs = ctx->last_stats.grid_b;
-    if (block) *block = 256;
+    if (block) *block = 32u * kDfsWarps;  // the enumeration (DFS) kernel's block
     return MBE_OK;
 }
