@@ -70,8 +70,8 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
                     mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
                     const EmitTarget* emit = nullptr);
 
-// Raw launchers of the two enumeration kernels (256 threads per block;
-// dfs_kernel runs kDfsWarps warps per block).
+// Raw launchers of the two enumeration kernels (root expansion: 256 threads
+// per block; DFS: kDfsWarps warps per block).
 cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s);
 cudaError_t launch_dfs(const EngineArgs& a, unsigned grid, cudaStream_t s);
 
