@@ -153,3 +153,18 @@ def test_alternative_paths_give_the_same_bicliques(engine, env):
                 os.environ[k] = v
     assert [(r.count, r.hash) for r in got] == [(r.count, r.hash) for r in base], env
     assert (em.count, em.hash, len(em.bicliques)) == (base[1].count, base[1].hash, base[1].count)
+
+
+def test_randomized_sweep_against_the_oracle(engine):
+    """150 random graphs: sizes 5..150 per side, densities 0.02..0.5, both
+    orientations.  On graphs this small thousands of warps wait for work,
+    so donation (pool copies and path replays) and the register search run
+    constantly."""
+    rng = np.random.default_rng(2026)
+    for i in range(150):
+        nr, nc = int(rng.integers(5, 151)), int(rng.integers(5, 151))
+        p = float(np.exp(rng.uniform(np.log(0.02), np.log(0.5))))
+        if nr * nc * p > 2500:  # keep the oracle's share of the test time small
+            p = 2500.0 / (nr * nc)
+        g = random_csr(rng, nr, nc, p)
+        _check(engine, g, "cuMBE" if i % 3 else "noRS")
