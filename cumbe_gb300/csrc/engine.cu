@@ -2175,8 +2175,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, expand_roots_kernel, kThreadsA, 0));
     MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occB, dfs_kernel, kThreadsB, 0));
     // root expansion at full occupancy (4 blocks per SM measured 23 -> 15 ms
-    // on the 94k x 30k graph against 2)
-    uint32_t gridA = (uint32_t)n_sm * (uint32_t)std::max(1, occA);
+    // on the 94k x 30k graph against 2), or within the share of the GPU a
+    // caller asked for (server slots that run side by side)
+    const int capA = cfg.blocks_per_sm ? (int)cfg.blocks_per_sm : occA;
+    uint32_t gridA = (uint32_t)n_sm * (uint32_t)std::max(1, std::min(occA, capA));
     uint32_t bpsm = cfg.blocks_per_sm ? cfg.blocks_per_sm : (uint32_t)std::max(1, occB);
     bpsm = std::min<uint32_t>(bpsm, (uint32_t)std::max(1, occB));
     uint32_t gridB = (uint32_t)n_sm * bpsm;
@@ -2294,13 +2296,15 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 #endif
 
     {
-        // No readback between the kernels when the scratch can be sized for
-        // the bound on any record (fewer than |R| candidates) within 4 GiB.
+        // One graph: no readback between the kernels when the scratch can be
+        // sized for the bound on any record (fewer than |R| candidates)
+        // within 4 GiB (small requests 0.191 -> 0.176 ms).  Many graphs keep
+        // the readback: measured faster for batches and server slots.
         const uint32_t scr_b = std::max<uint32_t>(maxNR, 32);
         size_t kc = 32;
         while (kc < scr_b) kc <<= 1;
         const size_t bytes = sizeof(uint32_t) * (size_t)nwarpsB * scratch_layout_words(maxW, scr_b, kc, cfg.emit != nullptr);
-        if (bytes <= (4ull << 30)) {
+        if (ng == 1 && bytes <= (4ull << 30)) {
             if ((st = eb.scratch.ensure(bytes))) return st;
             a.scratch = (uint32_t*)eb.scratch.ptr;
             a.scratch_dyn = 1;
