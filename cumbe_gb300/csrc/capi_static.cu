@@ -141,7 +141,7 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     const uint32_t scr_n = nR < 32 ? 32 : nR;
     uint32_t kc = 32;
     while (kc < scr_n) kc <<= 1;
-    const size_t sw = ((((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 6 * (size_t)kc) + 31) & ~(size_t)31;
+    const size_t sw = scratch_words(maxW, scr_n, kc, false);
     const uint32_t q_margin = 32 * kWarps + 1024;  // a donor pushes up to 31 tasks after its check
     const uint32_t task_cap = nR + q_margin + 4096;
 

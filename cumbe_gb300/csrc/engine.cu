@@ -161,25 +161,6 @@ __device__ __forceinline__ uint64_t side_hash(const GraphView& G, uint64_t sL, u
     return G.swapped ? mbe_pair_hash(sL, nl, sR, nr) : mbe_pair_hash(sR, nr, sL, nl);
 }
 
-// warp-level bitonic sort of u64 keys in memory (n a power of two >= 32)
-__device__ void warp_sort_u64(unsigned long long* k, uint32_t n) {
-    unsigned lane = lane_id();
-    for (uint32_t size = 2; size <= n; size <<= 1)
-        for (uint32_t j = size >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = lane; i < n; i += 32) {
-                uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    unsigned long long x = k[i], y = k[ixj];
-                    bool asc = (i & size) == 0;
-                    if ((x > y) == asc) {
-                        k[i] = y;
-                        k[ixj] = x;
-                    }
-                }
-            }
-            __syncwarp();
-        }
-}
 
 // register bitonic sort across the 32 lanes (ascending by lane)
 __device__ __forceinline__ unsigned long long warp_sort_reg(unsigned long long v) {
@@ -256,11 +237,6 @@ __device__ void block_exclusive_scan(uint32_t* a, uint32_t m, uint32_t* s_part) 
     __syncthreads();
 }
 
-__device__ __forceinline__ uint32_t next_pow2(uint32_t x) {
-    uint32_t p = 1;
-    while (p < x) p <<= 1;
-    return p;
-}
 
 // ---------------------------------------------------------------------------
 // Output stream (MBE_OPT_EMIT).  A counted biclique reserves room for its
@@ -758,6 +734,7 @@ struct WarpCtx {
     uint32_t* sLi;
     uint32_t* sNz;
     uint32_t* scrPack;     // 2 x kc words: srow, spos of a packed build too large for shared memory
+    uint32_t* scrHist;     // 32 maxW + 32 words: count histogram of a wide child's sorts
     uint32_t* scrAbs;      // scr_n words: ranks absorbed by the child being evaluated (output stream only)
     uint32_t scr_kc;       // key-array capacity of this launch's scratch layout
     uint32_t* sBucket;     // 64 words of shared memory: Q' then P' count buckets
@@ -1223,6 +1200,53 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     return out;
 }
 
+// Stable counting sort of n 64-bit keys by their high word (in [0, B)),
+// through tmp[n]; hist holds B words.  Replaces a bitonic sort of the same
+// keys when the high words are small counts: the order is the same.
+// Warp-collective.
+__device__ void warp_count_sort(unsigned long long* keys, uint32_t n, uint32_t B, uint32_t* hist,
+                                unsigned long long* tmp) {
+    const unsigned lane = lane_id();
+    for (uint32_t b = lane; b < B; b += 32) hist[b] = 0;
+    __syncwarp();
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t i = base + lane;
+        const bool v = i < n;
+        const uint32_t k = v ? (uint32_t)(keys[i] >> 32) : 0xFFFFFFFFu;
+        const unsigned grp = __match_any_sync(kFull, k);
+        if (v && (grp & lanemask_lt()) == 0) atomicAdd(&hist[k], (uint32_t)__popc(grp));
+    }
+    __syncwarp();
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < B; base += 32) {
+        const uint32_t b = base + lane;
+        const uint32_t c = b < B ? hist[b] : 0u;
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, inc, o);
+            if (lane >= (unsigned)o) inc += y;
+        }
+        if (b < B) hist[b] = carry + inc - c;
+        carry += __shfl_sync(kFull, inc, 31);
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t i = base + lane;
+        const bool v = i < n;
+        const unsigned long long key = v ? keys[i] : 0ull;
+        const uint32_t k = v ? (uint32_t)(key >> 32) : 0xFFFFFFFFu;
+        const unsigned grp = __match_any_sync(kFull, k);
+        const uint32_t off = v ? hist[k] : 0u;
+        if (v) tmp[off + __popc(grp & lanemask_lt())] = key;
+        __syncwarp();
+        if (v && (grp & lanemask_lt()) == 0) hist[k] = off + __popc(grp);
+        __syncwarp();
+    }
+    for (uint32_t i = lane; i < n; i += 32) keys[i] = tmp[i];
+    __syncwarp();
+}
+
 // Child record construction when |L_i| > 32 (rows stay word-sliced): the
 // Q part is sorted by count descending and reduced against a window of kept
 // rows, the P part sorted by count ascending.  Kept out of line: it is rare
@@ -1259,7 +1283,7 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
         uint32_t c = base + lane;
         uint32_t cc = c < xi ? wc.scrQcnt[c] : 0u;
         unsigned bal = __ballot_sync(kFull, cc > 0);
-        if (cc > 0) wc.scrKeysQ[m + __popc(bal & lanemask_lt())] = ((unsigned long long)(0xFFFFFFFFu - cc) << 32) | c;
+        if (cc > 0) wc.scrKeysQ[m + __popc(bal & lanemask_lt())] = ((unsigned long long)(li - cc) << 32) | c;
         m += __popc(bal);
     }
     __syncwarp();
@@ -1268,10 +1292,8 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
         k = warp_sort_reg(k);
         if (lane < m) wc.scrKeysQ[lane] = k;
     } else {
-        uint32_t N = next_pow2(m);
-        for (uint32_t t = m + lane; t < N; t += 32) wc.scrKeysQ[t] = kInvalidKey;
-        __syncwarp();
-        warp_sort_u64(wc.scrKeysQ, N);
+        // count descending (key li - count), parent order within a count
+        warp_count_sort(wc.scrKeysQ, m, li + 1, wc.scrHist, (unsigned long long*)wc.scrPack);
     }
     __syncwarp();
     // 5b. reduction, 32 candidates per step (same scheme as build_packed):
@@ -1312,10 +1334,8 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
         k = warp_sort_reg(k);
         if (lane < npp) wc.scrKeysP[lane] = k;
     } else {
-        uint32_t N = next_pow2(npp);
-        for (uint32_t t = npp + lane; t < N; t += 32) wc.scrKeysP[t] = kInvalidKey;
-        __syncwarp();
-        warp_sort_u64(wc.scrKeysP, N);
+        // count ascending, parent order within a count (keys in scan order)
+        warp_count_sort(wc.scrKeysP, npp, li + 1, wc.scrHist, (unsigned long long*)wc.scrPack);
     }
     __syncwarp();
 
@@ -1536,7 +1556,13 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
         PROF_ADD(wc.prof, kProfBuild);
         return out;
     }
+#ifdef MBE_PROFILE
+    const long long c0g = clock64();
+#endif
     out = build_general(a, G, nd, xi, li, nnz, Li, Nz, npp, nR2, sR2, known_max, wc, acc);
+#ifdef MBE_PROFILE
+    PROF_VAL(wc.prof, kProfGeneral, clock64() - c0g);
+#endif
     return out;
 }
 
@@ -1841,17 +1867,15 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
     WarpCtx wc;
     wc.arena = a.arena + gw * a.arena_words;
     wc.arena_top = 0;
-    // scratch layout: Li[max_W] Nz[max_W] qcnt[scr_n] | keysP[kc] keysQ[kc]
-    // (u64) | srow/spos[2 kc] | absorbed[scr_n] (output stream), kc = the
-    // power of two >= scr_n; scr_n from the largest root record of the chunk
+    // scratch layout (scratch_words): scr_n from the largest root record of
+    // the chunk, kc the power of two >= scr_n
     uint32_t scr_n = a.scr_n, kc = a.scr_kc;
     size_t sw = a.scratch_words;
     if (a.scratch_dyn) {
         scr_n = max(*(const volatile uint32_t*)a.max_n, 32u);
         kc = 32;
         while (kc < scr_n) kc <<= 1;
-        sw = ((((2 * (size_t)a.max_W + scr_n + 1) & ~(size_t)1) + 6 * (size_t)kc + (a.emit ? scr_n : 0)) + 31) &
-             ~(size_t)31;
+        sw = scratch_words(a.max_W, scr_n, kc, a.emit != 0);
     }
     uint32_t* scr = a.scratch + gw * sw;
     wc.scrLi = scr;
@@ -1861,7 +1885,8 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
     wc.scrKeysP = (unsigned long long*)(scr + koff);
     wc.scrKeysQ = wc.scrKeysP + kc;
     wc.scrPack = (uint32_t*)(wc.scrKeysQ + kc);
-    wc.scrAbs = wc.scrPack + 2 * (size_t)kc;
+    wc.scrHist = wc.scrPack + 2 * (size_t)kc;
+    wc.scrAbs = wc.scrHist + 32 * (size_t)a.max_W + 32;
     wc.scr_kc = kc;
     wc.sLi = sLi[warp];
     wc.sNz = sNz[warp];
@@ -2139,12 +2164,6 @@ struct Ctrl {
 };
 }  // namespace
 
-// Words of one warp's DFS scratch for records of up to scr_n candidates
-// (kc = the power of two >= scr_n); the DFS kernel lays it out the same way.
-static size_t scratch_layout_words(uint32_t maxW, uint32_t scr_n, size_t kc, bool emit) {
-    return align_up(((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 6 * kc + (emit ? scr_n : 0), 32);
-}
-
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
                       const std::vector<const DeviceGraph*>& gs, const std::vector<uint2>& roots,
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io) {
@@ -2303,7 +2322,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         const uint32_t scr_b = std::max<uint32_t>(maxNR, 32);
         size_t kc = 32;
         while (kc < scr_b) kc <<= 1;
-        const size_t bytes = sizeof(uint32_t) * (size_t)nwarpsB * scratch_layout_words(maxW, scr_b, kc, cfg.emit != nullptr);
+        const size_t bytes = sizeof(uint32_t) * (size_t)nwarpsB * scratch_words(maxW, scr_b, kc, cfg.emit != nullptr);
         if (ng == 1 && bytes <= (4ull << 30)) {
             if ((st = eb.scratch.ensure(bytes))) return st;
             a.scratch = (uint32_t*)eb.scratch.ptr;
@@ -2375,7 +2394,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
                 while (kc < scr_n) kc <<= 1;
-                size_t sw = scratch_layout_words(maxW, scr_n, kc, cfg.emit != nullptr);
+                size_t sw = scratch_words(maxW, scr_n, kc, cfg.emit != nullptr);
                 if ((st = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB * sw))) return st;
                 a.scratch = (uint32_t*)eb.scratch.ptr;
                 a.scratch_words = (uint32_t)sw;
@@ -2464,7 +2483,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         MBE_CUDA_TRY(cudaMemcpy(hp, a.prof, sizeof hp, cudaMemcpyDeviceToHost));
         static const char* names[] = {"pop", "replay", "donate", "prefilter", "qscan", "expand", "build", "solve",
                                       "b.gather", "b.sort", "b.reduce", "b.write", "sum xi", "sum m", "sum nq2", "sum npp",
-                                      "small eval", "small pre", "small bld"};
+                                      "small eval", "small pre", "small bld", "general"};
         unsigned long long tot = 0;
         for (int q = 0; q < kProfMain; q++) tot += hp[2 * q];
         for (int q = 0; q < kProfSections; q++)

@@ -91,6 +91,7 @@ enum : int {
     kProfSmallEval,      // evaluations (cycles) of children of packed records with <= 32 rows
     kProfSmallPre,       // prefilter batches (cycles) on such records
     kProfSmallBuild,     // builds of packed records with <= 32 rows (cycles)
+    kProfGeneral,        // builds of unpacked (|L| > 32) child records (cycles, events)
     kProfSections,
     kProfSlots = 2 * kProfSections,
     kProfBins = 512,           // idle-time histogram over kernel time
@@ -111,6 +112,17 @@ __host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n, bool pa
 // only), stored right after the bit rows at word offset record_words().
 __host__ __device__ inline uint64_t record_words_r(uint32_t W, uint32_t n, bool packed, uint32_t nr) {
     return record_words(W, n, packed) + pad4(nr);
+}
+
+// Words of one DFS warp's scratch for records of up to scr_n candidates
+// (kc = the power of two >= scr_n, maxW = the widest L in words):
+//   Li[maxW] Nz[maxW] qcnt[scr_n] (padded to even) | keysP[kc] keysQ[kc]
+//   (u64) | pack[2 kc] | hist[32 maxW + 32] | absorbed[scr_n] (output stream)
+// The DFS kernel lays it out the same way.
+__host__ __device__ inline size_t scratch_words(uint32_t maxW, uint32_t scr_n, size_t kc, bool emit) {
+    const size_t w = ((2 * (size_t)maxW + scr_n + 1) & ~(size_t)1) + 6 * kc + 32 * (size_t)maxW + 32 +
+                     (emit ? scr_n : 0);
+    return (w + 31) & ~(size_t)31;
 }
 
 // A unit of work: children [begin, end) of the node reached from the pool
