@@ -967,6 +967,17 @@ __device__ __forceinline__ uint32_t packed_row(const uint32_t* M, uint32_t n, co
     return row;
 }
 
+// Row of candidate c restricted to L_i, as the Q' gather and reduction use
+// it: raw (M & Li[0]) when L_i spans one word, since counts and subset tests
+// are the same on raw and packed masks; packed otherwise.  A raw row is
+// packed (compress32 with plan0) only if it is kept.
+__device__ __forceinline__ uint32_t gather_row(const uint32_t* M, uint32_t n, const uint32_t* Nz,
+                                               const uint32_t* Li, uint32_t nnz, uint32_t c,
+                                               const CompressPlan& plan0) {
+    if (nnz == 1) return M[(size_t)Nz[0] * n + c] & plan0.mask;
+    return packed_row(M, n, Nz, Li, nnz, c, plan0);
+}
+
 // Position of the k-th (0-based) set bit of x (k < popc(x)), by halving.
 __device__ __forceinline__ uint32_t select32(uint32_t x, uint32_t k) {
     uint32_t pos = 0, c;
@@ -1026,7 +1037,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
             uint32_t c = base + 32 * q + lane;
-            r[q] = c < xi ? packed_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
+            r[q] = c < xi ? gather_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
         }
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
@@ -1045,7 +1056,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
             uint32_t c = base + 32 * q + lane;
-            r[q] = c < xi ? packed_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
+            r[q] = c < xi ? gather_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
         }
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
@@ -1076,10 +1087,15 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
         uint32_t idx = base + lane;
         bool valid = idx < m;
         uint32_t r = valid ? srow[idx] : 0u, p = valid ? spos[idx] : 0u;
+        // lanes >= nk hold 0, which dominates no valid (non-zero) row
         bool dom = !valid;
-        for (uint32_t j = 0; j < nk; j++) {
-            uint32_t kr = __shfl_sync(kFull, kept_row, j);
-            dom = dom || (r & ~kr) == 0;
+        for (uint32_t j = 0; j < nk; j += 4) {
+#pragma unroll
+            for (uint32_t u = 0; u < 4; u++) {
+                uint32_t kr = __shfl_sync(kFull, kept_row, j + u);
+                dom = dom || (r & ~kr) == 0;
+            }
+            if (__all_sync(kFull, dom)) break;
         }
         unsigned pending = __ballot_sync(kFull, !dom), keep = 0;
         while (pending) {
@@ -1168,7 +1184,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     for (uint32_t t = lane; t < nq2; t += 32) {
         cand2[t] = R.cand[spos[t]];
         cnt2[t] = 0;
-        M2[t] = srow[t];
+        M2[t] = nnz == 1 ? compress32(srow[t], plan0) : srow[t];
     }
     for (uint32_t base = 0; base < npp; base += 32) {
         uint32_t t = base + lane;
