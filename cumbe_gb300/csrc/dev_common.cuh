@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 
 #include "mbe.h"
 #include "mbe_internal.h"
@@ -24,11 +25,23 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 
+// Sum over the warp of an integer, wrapping like the type: one redux.sync
+// for 32-bit values; for 64-bit values three independent ones (the high
+// words mod 2^32 and the two 16-bit halves of the low words, whose totals
+// stay below 2^21), recombined mod 2^64.
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-    return v;
+    static_assert(std::is_integral<T>::value && (sizeof(T) == 4 || sizeof(T) == 8), "32/64-bit integers");
+    if constexpr (sizeof(T) == 4) {
+        return (T)__reduce_add_sync(kFull, (uint32_t)v);
+    } else {
+        const uint64_t u = (uint64_t)v;
+        const uint32_t lo = (uint32_t)u;
+        const uint32_t shi = __reduce_add_sync(kFull, (uint32_t)(u >> 32));
+        const uint32_t s0 = __reduce_add_sync(kFull, lo & 0xFFFFu);
+        const uint32_t s1 = __reduce_add_sync(kFull, lo >> 16);
+        return (T)(((uint64_t)shi << 32) + ((uint64_t)s1 << 16) + s0);
+    }
 }
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
