@@ -970,11 +970,12 @@ __device__ __forceinline__ uint32_t packed_row(const uint32_t* M, uint32_t n, co
 // Row of candidate c restricted to L_i, as the Q' gather and reduction use
 // it: raw (M & Li[0]) when L_i spans one word, since counts and subset tests
 // are the same on raw and packed masks; packed otherwise.  A raw row is
-// packed (compress32 with plan0) only if it is kept.
-__device__ __forceinline__ uint32_t gather_row(const uint32_t* M, uint32_t n, const uint32_t* Nz,
-                                               const uint32_t* Li, uint32_t nnz, uint32_t c,
+// packed (compress32 with plan0) only if it is kept.  M0 is the row strip of
+// L_i's one word.
+__device__ __forceinline__ uint32_t gather_row(const uint32_t* M, const uint32_t* M0, uint32_t n,
+                                               const uint32_t* Nz, const uint32_t* Li, uint32_t nnz, uint32_t c,
                                                const CompressPlan& plan0) {
-    if (nnz == 1) return M[(size_t)Nz[0] * n + c] & plan0.mask;
+    if (nnz == 1) return M0[c] & plan0.mask;
     return packed_row(M, n, Nz, Li, nnz, c, plan0);
 }
 
@@ -1025,6 +1026,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t* M = R.M;
     const CompressPlan plan0 = compress_plan(Li[0]);
+    const uint32_t* M0 = M + (size_t)Nz[0] * n;
     ChildOut out{nullptr, 0, 0};
     PROF_T0();
     // Q' = rows of Q u P[0..i) meeting L_i, by count descending (key li -
@@ -1037,7 +1039,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
             uint32_t c = base + 32 * q + lane;
-            r[q] = c < xi ? gather_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
+            r[q] = c < xi ? gather_row(M, M0, n, Nz, Li, nnz, c, plan0) : 0u;
         }
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
@@ -1056,7 +1058,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
             uint32_t c = base + 32 * q + lane;
-            r[q] = c < xi ? gather_row(M, n, Nz, Li, nnz, c, plan0) : 0u;
+            r[q] = c < xi ? gather_row(M, M0, n, Nz, Li, nnz, c, plan0) : 0u;
         }
 #pragma unroll
         for (int q = 0; q < kUnrollG; q++) {
@@ -1198,7 +1200,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
             uint32_t c = nq + (uint32_t)key;
             cand2[dst] = R.cand[c];
             cnt2[dst] = cc;
-            M2[dst] = packed_row(M, n, Nz, Li, nnz, c, plan0);
+            M2[dst] = nnz == 1 ? compress32(M0[c], plan0) : packed_row(M, n, Nz, Li, nnz, c, plan0);
         }
         __syncwarp();
         if (v && (grp & lanemask_lt()) == 0) sbp[cc] = off + __popc(grp);
@@ -1473,6 +1475,11 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
     __syncwarp();
     if (!known_max) acc.nodes++;
     acc.words += W;
+    // one-word L_i (the common case): its row strip and mask in registers,
+    // since the scans below store to shared memory and the compiler would
+    // otherwise reload Nz[0] and Li[0] before every chunk
+    const uint32_t* M0 = M + (size_t)(nnz ? Nz[0] : 0u) * n;
+    const uint32_t L0 = Li[0];
 
     // 2. maximality against Q u P[0..i); counts kept for Q'
     if (!known_max) {
@@ -1482,7 +1489,10 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
             uint32_t c = base + lane;
             uint32_t cc = 0;
             if (c < xi) {
-                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+                if (nnz == 1)
+                    cc = __popc(M0[c] & L0);
+                else
+                    for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
                 wc.scrQcnt[c] = cc;
             }
             unsigned full = __ballot_sync(kFull, c < xi && cc == li);
@@ -1512,8 +1522,12 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
         for (int h2 = 0; h2 < kUnrollE; h2++) {
             uint32_t c = base + 32 * h2 + lane;
             uint32_t cc = 0;
-            if (c < n)
-                for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+            if (c < n) {
+                if (nnz == 1)
+                    cc = __popc(M0[c] & L0);
+                else
+                    for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
+            }
             cc2[h2] = cc;
         }
 #pragma unroll
