@@ -1629,7 +1629,12 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, R
 
 // Splits the remaining children of the shallowest frame with at least
 // donate_min of them among the donor and up to 31 waiting warps (one task
-// per lane, equal shares; the donor keeps the lowest indices).  A frame whose
+// per lane, equal shares; the donor keeps the lowest indices).  Children the
+// batch prefilter found maximal and that still wait in a frame's pmask count
+// too, and go first: a frame with two or more of them gives its highest ones
+// away as one-child tasks (the receiver re-tests their maximality).  Without
+// this a warp holding a batch of up to 31 heavy children could not share them
+// (bench graph 287 -> 256 ms, all of it in the closing phase).  A frame whose
 // record is in the node pool is shared by pointer.  A frame whose record lives
 // in this warp's arena is copied once into the pool when it fits (pool below
 // 60%: small records into this warp's slab, larger ones by a direct
@@ -1647,14 +1652,19 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
             Frame fr = frames[f];
             uint32_t* nd = (uint32_t*)fr.node;
             bool in_arena = nd >= wc.arena && nd < wc.arena + a.arena_words;
-            ok = fr.end > fr.next && fr.end - fr.next >= a.donate_min && (!in_arena || f <= (int)kMaxPath);
+            ok = ((fr.end > fr.next && fr.end - fr.next >= a.donate_min) || __popc(fr.pmask) >= 2) &&
+                 (!in_arena || f <= (int)kMaxPath);
         }
         unsigned bal = __ballot_sync(kFull, ok);
         if (bal) k = base + __ffs(bal) - 1;
     }
     if (k < 0) return;
     Frame fr = frames[k];
-    const uint32_t rem = fr.end - fr.next;
+    // children the batch prefilter found maximal and that wait in pmask go
+    // first (they precede [next, end)); each one given away is its own task
+    const uint32_t npend = __popc(fr.pmask);
+    const bool from_mask = npend >= 2;
+    const uint32_t rem = from_mask ? npend : fr.end - fr.next;
     const uint32_t pieces = min(min(waiters, 31u), rem - 1);  // tasks given away
     if (pieces == 0) return;
     const uint32_t share = rem / (pieces + 1);
@@ -1718,11 +1728,23 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
         t.plen = (uint32_t)k;
     }
     for (int j = 0; j < (int)t.plen; j++) t.path[j] = __shfl_sync(kFull, pe, j);
-    if (lane == 0) frames[k].end = mid;
-    if (lane < pieces) {
-        t.begin = mid + lane * share;
-        t.end = t.begin + share;
-        push_task(a, t);
+    if (from_mask) {
+        // the highest `pieces` pending children leave; the donor keeps the
+        // lower ones (select32 gives the position of a set bit by rank)
+        const uint32_t first = select32(fr.pmask, npend - pieces);
+        if (lane == 0) frames[k].pmask = fr.pmask & ((1u << first) - 1u);
+        if (lane < pieces) {
+            t.begin = fr.mbase + select32(fr.pmask, npend - pieces + lane);
+            t.end = t.begin + 1;
+            push_task(a, t);
+        }
+    } else {
+        if (lane == 0) frames[k].end = mid;
+        if (lane < pieces) {
+            t.begin = mid + lane * share;
+            t.end = t.begin + share;
+            push_task(a, t);
+        }
     }
     __syncwarp();
 }
