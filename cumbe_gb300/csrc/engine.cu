@@ -1868,7 +1868,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
                 sR = sR2;
             }
         }
-        if ((++iter & 15u) == 0) {
+        if ((++iter & 63u) == 0) {
             if (lane == 0 && (iter & 1023u) == 0) atomicAdd(a.progress, 1ull);
             if (ld_volatile(a.error)) break;
             if (donate) {
@@ -2140,7 +2140,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                 }
                 __syncwarp();
             }
-            if (ld_volatile(a.error)) break;
+            if ((evals & 7u) == 0 && ld_volatile(a.error)) break;
         }
         flush_acc(a, graph, acc);
         if (lane == 0) {
