@@ -2219,8 +2219,8 @@ struct Ctrl {
 // Shared-memory carveout for the DFS kernel: the smallest share of the SM's
 // unified memory that holds MBE_DFS_MIN_BLOCKS blocks, raised until the
 // occupancy query confirms that many.  The rest stays L1, which the record
-// scans run from: 64 KB of shared memory measured faster than the driver's
-// own choice (bench graph 303.9 -> 294.9 ms, 588-graph batch 737 -> 696 ms).
+// scans run from: 64 KB of shared memory measured faster than the default
+// carveout (bench graph 303.9 -> 294.9 ms, 588-graph batch 737 -> 696 ms).
 static cudaError_t set_dfs_carveout() {
     cudaFuncAttributes fa{};
     cudaError_t e = cudaFuncGetAttributes(&fa, dfs_kernel);
