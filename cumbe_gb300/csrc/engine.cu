@@ -1598,30 +1598,61 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
 
 // Maximality of up to 32 consecutive children of a record with one-word
 // rows, one lane per child: lane j takes child base + j and walks the rows
-// of Q u P[0..i) in order until one covers L_i.  At every step all lanes
-// read the same row (one broadcast load), eight rows per step.  Returns the
-// children no row covers.  Exact: the same test eval_child makes.
+// of Q u P[0..i) that can cover L_i, in order, until one does.  At every
+// step all lanes read the same row (one broadcast load), eight rows per
+// step.  Returns the children no row covers.  Exact: the same test
+// eval_child makes, skipping only rows whose count rules them out.
 __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, ResultAcc& acc) {
     const unsigned lane = lane_id();
     const bool active = lane < nb;
-    const uint32_t xi = R.nq + base + lane;
+    const uint32_t nq = R.nq;
+    const uint32_t xi = nq + base + lane;
     const uint32_t Li = active ? (R.Lm[0] & R.M[xi]) : 0u;
     const uint32_t lim = active ? xi : 0u;
+    // A row covering L_i holds at least |L_i| of L's bits.  P rows are in
+    // ascending count order, so none of P[0..i) has more than |L_i| and only
+    // the run with exactly |L_i| can cover L_i: the lane scans all of Q,
+    // then P from the first row of that run (found by binary search).
+    uint32_t plo = lim;
+    if (active) {
+        const uint32_t li = __popc(Li);
+        uint32_t lo = nq, hi = xi;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (R.cnt[mid] < li)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        plo = lo;
+    }
     bool covered = !active;
-    uint32_t c = 0;
-    while (__any_sync(kFull, !covered && c < lim)) {
+    uint32_t seen = 0;  // rows this lane tested
+    const uint32_t qlim = min(nq, lim);
+    for (uint32_t c = 0; __any_sync(kFull, !covered && c < qlim); c += kUnrollP) {
 #pragma unroll
         for (uint32_t u = 0; u < (uint32_t)kUnrollP; u++) {
-            uint32_t cc = c + u;
-            if (!covered && cc < lim) {
-                uint32_t r = R.M[cc];
+            const uint32_t cc = c + u;
+            if (!covered && cc < qlim) {
+                const uint32_t r = R.M[cc];
                 covered = (r & Li) == Li;
+                seen++;
             }
         }
-        c += kUnrollP;
     }
-    unsigned long long scanned = active ? min(c, lim) : 0u;
-    scanned = warp_sum(scanned);
+    const uint32_t p0 = __reduce_min_sync(kFull, covered ? 0xFFFFFFFFu : plo);
+    for (uint32_t c = p0; __any_sync(kFull, !covered && c < lim); c += kUnrollP) {
+#pragma unroll
+        for (uint32_t u = 0; u < (uint32_t)kUnrollP; u++) {
+            const uint32_t cc = c + u;
+            if (!covered && cc >= plo && cc < lim) {
+                const uint32_t r = R.M[cc];
+                covered = (r & Li) == Li;
+                seen++;
+            }
+        }
+    }
+    unsigned long long scanned = warp_sum((unsigned long long)seen);
     acc.words += scanned + nb;
     acc.nodes += nb;
     return __ballot_sync(kFull, active && !covered);
