@@ -73,10 +73,32 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
-def replicas_value(count_per_step, world, ms_per_step):
-    """Whole-job bicliques/s of `world` replicas that each enumerate
-    count_per_step bicliques per step, timed by the slowest replica."""
-    return count_per_step * world / (ms_per_step / 1000.0)
+def sum_over_ranks(x, world, device):
+    """The sum of the ranks' integer values of x (each rank's share of the
+    bicliques); x itself on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return int(t.item())
+
+
+def shard_of(rank, world):
+    """Root sample of one rank: processing positions rank, rank + world, ...
+    (round-robin over the degree order, so every rank gets the same mix of
+    light and heavy roots).  The shards partition the roots, so the ranks'
+    counts (and hashes, a wrapping sum) add up to the whole graph's."""
+    if world <= 1:
+        return {}
+    return {"root_begin": rank, "root_stride": world}
+
+
+def sharded_value(total_count_per_step, ms_per_step):
+    """Whole-job bicliques/s: the bicliques all ranks found in one step,
+    divided by the slowest rank's step time."""
+    return total_count_per_step / (ms_per_step / 1000.0)
 
 
 def peak_hbm():
@@ -151,11 +173,11 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def cpu_baseline(g, wl, threads, stride_mult=1):
+def cpu_baseline(csr, wl, threads, stride_mult=1):
     """The oracle port on the host cores over a stride sample of the roots."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    nr, nc, rp, ci = g.csr()
+    nr, nc, rp, ci = csr
     stride = wl["cpu_stride"] * stride_mult
     t0 = time.perf_counter()
     r = oracle.ref_enumerate_sampled(nr, nc, rp, ci, stride, threads=threads)
@@ -266,20 +288,22 @@ def stress_leg(eng):
 
 
 def run_reference(args, wl, rank, world):
-    """--impl reference: the CPU restatement of the reference's search."""
+    """--impl reference: the CPU restatement of the reference's search, on
+    a graph built by the oracle's own copy of the generator (this arm never
+    loads the product library)."""
     if rank != 0:
         return
-    import cumbe_gb300 as cm
-    from cumbe_gb300 import build as b
-    b.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
     params = {k: v for k, v in wl.items() if k != "cpu_stride"}
-    g = cm.Graph.generate(**params)
+    csr = oracle.generate(**params)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_baseline(g, wl, threads, stride_mult=10)  # warm caches on a 10x thinner sample
+        cpu_baseline(csr, wl, threads, stride_mult=10)  # warm caches on a 10x thinner sample
     tot_c, tot_t = 0, 0.0
     for _ in range(args.steps):
-        r, dt, stride = cpu_baseline(g, wl, threads)
+        r, dt, stride = cpu_baseline(csr, wl, threads)
         tot_c += r.count
         tot_t += dt
     v = tot_c / tot_t if tot_t > 0 else 0.0
@@ -296,6 +320,63 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def reference_gpu_leg(eng, workload="power_law_94k_30k_e100k"):
+    """The reference's own cuMBE kernel (compiled from its unmodified
+    sources into oracle/_ref by oracle/build_ref.py, driven by
+    oracle/ref_runner) on one graph, timed as the reference times it: CUDA
+    events around its cooperative launch.  This engine runs the same graph
+    for the same-config ratio.  None when the reference build is absent."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import re
+    import tempfile
+    import build_ref
+    import cumbe_gb300 as cm
+    try:
+        built = build_ref.build()
+    except Exception as e:  # no CUDA headers / compiler on this host
+        return {"unavailable": f"reference runner build failed: {e}"}
+    if not built.get("cubin") or not built.get("runner"):
+        return {"unavailable": "the reference's kernels were not built here (oracle/_ref/cumbe_ref.cubin missing)"}
+    params = {k: v for k, v in WORKLOADS[workload].items() if k != "cpu_stride"}
+    g = cm.Graph.generate(**params)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "g.bi")
+        g.write_bi(path)
+        r = subprocess.run([built["runner"], built["cubin"], path, "cuMBE"], capture_output=True, text=True,
+                           timeout=300)
+    m = re.search(r"maximal bicliques: (-?\d+)", r.stdout)
+    t = re.search(r"runtime \(s\): ([0-9.eE+-]+)", r.stdout)
+    if r.returncode != 0 or not m or not t:
+        return {"unavailable": f"reference runner failed (rc {r.returncode}): {r.stderr[-300:]}"}
+    ref_count, ref_s = int(m.group(1)), float(t.group(1))
+    eng.enumerate(g)  # warm-up (upload, transpose)
+    mine = eng.enumerate(g)
+    eng.release(g)
+    return {"workload": workload, **params, "variant": "cuMBE",
+            "reference_count": ref_count, "reference_kernel_s": ref_s,
+            "reference_bicliques_per_s": ref_count / ref_s if ref_s > 0 else None,
+            "engine_count": mine.count, "engine_ms": mine.ms,
+            "engine_bicliques_per_s": mine.count / (mine.ms / 1e3) if mine.ms > 0 else None,
+            "counts_equal": ref_count == mine.count % (1 << 32) if ref_count >= 0 else None,
+            "speedup_kernel_time": ref_s * 1e3 / mine.ms if mine.ms > 0 else None,
+            "how": "reference: its kernels compiled from its own sources for sm_103a, launched cooperatively by "
+                   "oracle/ref_runner (a restatement of src/main.cu's host steps), event time of the launch; "
+                   "engine: root expansion + DFS event time, graph resident"}
+
+
+# Frozen numerator of the dfs_kernel roofline, per workload: 4 B x the
+# 32-bit words of set data that the kernel's node evaluations must read
+# (row words of each candidate scanned, L_i words, written child records),
+# as the kernel's word counter defined them when these figures were fixed
+# (1.2040e10 words per launch on the 293,000-edge graph).  The
+# figure is held fixed so that a kernel that skips work shows as a higher
+# achieved rate on the same work, never as a smaller numerator; the live
+# counter of the running build is reported beside it.
+FROZEN_ALGORITHMIC_BYTES = {
+    "power_law_94k_30k": 48_160_205_850,
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,6 +389,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -324,12 +406,14 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     b.build()
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     params = {k: v for k, v in wl.items() if k != "cpu_stride"}
     g = cm.Graph.generate(**params)
     info = g.info()
+    shard = shard_of(rank, world)
     eng = cm.Engine(local)
     eng.upload(g)
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
     def barrier():
         torch.cuda.synchronize()
@@ -337,7 +421,7 @@ def main():
             torch.distributed.barrier()
 
     for _ in range(args.warmup):
-        r0 = eng.enumerate(g, args.variant)
+        r0 = eng.enumerate(g, args.variant, **shard)
     # ---- device-resident throughput (value) ----
     c0 = eng.counters()
     sampler = ClockSampler(local)
@@ -348,7 +432,7 @@ def main():
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        r = eng.enumerate(g, args.variant)
+        r = eng.enumerate(g, args.variant, **shard)
         results.append(r)
         tot_count += r.count
         tot_ms += r.ms
@@ -359,8 +443,10 @@ def main():
     c1 = eng.counters()
     if any((x.count, x.hash) != (r0.count, r0.hash) for x in results):
         raise SystemExit("enumeration results differ between steps")
-    ms_step = max_over_ranks(tot_ms / args.steps, world, f"cuda:{local}")
-    value = replicas_value(tot_count / args.steps, world, ms_step)
+    ms_step = max_over_ranks(tot_ms / args.steps, world, dev)
+    job_count = sum_over_ranks(r0.count, world, dev)  # every rank's share of one step
+    job_hash = sum_over_ranks(r0.hash - (1 << 64) if r0.hash >= (1 << 63) else r0.hash, world, dev) % (1 << 64)
+    value = sharded_value(job_count, ms_step)
 
     # ---- end to end through the C ABI from host buffers (e2e) ----
     e_c0 = eng.counters()
@@ -369,38 +455,50 @@ def main():
     for _ in range(args.steps):
         eng.release(g)
         t0 = time.perf_counter()
-        r = eng.enumerate(g, args.variant)  # upload (H2D + transpose) + enumerate + D2H
+        r = eng.enumerate(g, args.variant, **shard)  # upload (H2D + transpose) + enumerate + D2H
         e2e_wall += time.perf_counter() - t0
         e2e_count += r.count
     barrier()
     e_c1 = eng.counters()
-    e2e = {"value": e2e_count * world / e2e_wall, "unit": "bicliques/s",
+    e2e_s = max_over_ranks(e2e_wall, world, dev)
+    e2e = {"value": sum_over_ranks(e2e_count, world, dev) / e2e_s, "unit": "bicliques/s",
            "h2d_bytes_per_step": (e_c1["h2d"] - e_c0["h2d"]) // args.steps,
            "d2h_bytes_per_step": (e_c1["d2h"] - e_c0["d2h"]) // args.steps}
 
     # ---- roofline of the dominant kernel (dfs_kernel) ----
     peak, peak_kind = peak_hbm()
-    achieved = (tot_words * 4) / (tot_dfs_ms / 1000.0) / 1e9 if tot_dfs_ms > 0 else 0.0
+    launch_ms = tot_dfs_ms / args.steps
+    live_bytes = tot_words * 4 // args.steps
+    frozen = FROZEN_ALGORITHMIC_BYTES.get(args.workload) if world == 1 else None
+    alg_bytes = frozen if frozen is not None else live_bytes
+    achieved = alg_bytes / (launch_ms / 1000.0) / 1e9 if launch_ms > 0 else 0.0
     traffic = profile_traffic(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind, "kernel": "dfs_kernel",
-                "algorithmic_bytes_per_launch": tot_words * 4 // args.steps,
-                "launch_ms": tot_dfs_ms / args.steps,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "numerator": "frozen per workload" if frozen is not None else "live kernel word counter",
+                "live_counter_bytes_per_launch": live_bytes,
+                "launch_ms": launch_ms,
+                "dram_bytes_per_launch_ncu": traffic,
                 # from the committed ncu summaries: the kernel is L1/L2- and latency-bound
                 "l2_hit_rate": profile_value(args.workload, "l2_hit_rate"),
                 "int_pipe_active": profile_value(args.workload, "int_pipe_active")}
 
     line = {"metric": "maximal bicliques/sec", "value": value, "unit": "bicliques/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic",
             "config": {"workload": args.workload, **params, "variant": args.variant,
                        "l2": "flushed before every timed step (512 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "bicliques_per_step": r0.count, "hash": f"{r0.hash:#018x}",
+                       "parallelism": (f"roots sharded round-robin over {world} ranks (positions r, r+{world}, ...)"
+                                       if world > 1 else "single GPU"),
+                       "bicliques_per_step": job_count, "hash": f"{job_hash:#018x}",
                        "tree_nodes_per_step": r0.nodes, "n_edges": info["n_edges"]},
             "e2e": e2e, "roofline": roofline,
             "gpu_launches": c1["launches"] - c0["launches"],
             "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_leg(eng)
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_leg(eng)
     if rank == 0 and not args.no_served:
@@ -411,7 +509,7 @@ def main():
         line["stress"] = stress_leg(eng)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rc, dt, stride = cpu_baseline(g, wl, threads)
+        rc, dt, stride = cpu_baseline(g.csr(), wl, threads)
         line["cpu_baseline"] = {"value": rc.count / dt if dt > 0 else 0.0, "unit": "bicliques/s", "cores": threads,
                                 "kind": "port",
                                 "sample": f"every {stride}-th root (stride sample) of the same graph: "

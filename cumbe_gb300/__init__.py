@@ -57,7 +57,9 @@ class _Opts(ctypes.Structure):
                 ("donate_min", ctypes.c_uint32), ("stack_words", ctypes.c_uint32),
                 ("emit_offsets", ctypes.POINTER(ctypes.c_uint32)), ("emit_ids", ctypes.POINTER(ctypes.c_uint32)),
                 ("emit_nrows", ctypes.POINTER(ctypes.c_uint32)), ("emit_cap_bicliques", ctypes.c_uint64),
-                ("emit_cap_ids", ctypes.c_uint64)]
+                ("emit_cap_ids", ctypes.c_uint64), ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32),
+                ("root_stride", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("wait_timeout_ns", ctypes.c_uint64)]
 
 
 class _Result(ctypes.Structure):
@@ -245,7 +247,11 @@ class Graph:
         return cls(h)
 
 
-def _opts(flags=0, min_rows=0, min_cols=0, donate_min=0, blocks_per_sm=0, stack_words=0) -> _Opts:
+def _opts(flags=0, min_rows=0, min_cols=0, donate_min=0, blocks_per_sm=0, stack_words=0, warps_per_block=0,
+          root_begin=0, root_end=0, root_stride=0, wait_timeout_ns=0) -> _Opts:
+    """mbe_opts: thresholds, tuning, the root sample (positions
+    [root_begin, root_end) step root_stride of the processing order) and
+    the device-wait limit."""
     o = _Opts()
     o.flags = flags
     o.min_rows = min_rows
@@ -253,6 +259,11 @@ def _opts(flags=0, min_rows=0, min_cols=0, donate_min=0, blocks_per_sm=0, stack_
     o.donate_min = donate_min
     o.blocks_per_sm = blocks_per_sm
     o.stack_words = stack_words
+    o.warps_per_block = warps_per_block
+    o.root_begin = root_begin
+    o.root_end = root_end
+    o.root_stride = root_stride
+    o.wait_timeout_ns = wait_timeout_ns
     return o
 
 

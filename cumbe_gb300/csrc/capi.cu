@@ -59,12 +59,25 @@ EngineConfig make_config(mbe_variant v, const mbe_opts* o, bool swapped) {
         if (o->donate_min) c.donate_min = o->donate_min;
         if (o->blocks_per_sm) c.blocks_per_sm = o->blocks_per_sm;
         if (o->stack_words) c.arena_words = (o->stack_words + 3u) & ~3u;
+        if (o->wait_timeout_ns) c.timeout_ns = o->wait_timeout_ns;
     }
     if (const char* env = std::getenv("MBE_POOL_MB")) {
         unsigned long long mb = std::strtoull(env, nullptr, 10);
         if (mb) c.pool_words = mb * (1ull << 20) / 4;
     }
     return c;
+}
+
+// Rejects option values the engine cannot honour.
+mbe_status check_opts(const mbe_opts* o) {
+    if (!o) return MBE_OK;
+    if (o->warps_per_block && o->warps_per_block != (uint32_t)kDfsWarps)
+        return fail(MBE_ERR_INVALID_ARG, "warps_per_block must be 0 or " + std::to_string(kDfsWarps) +
+                                             " (the DFS kernel's compiled block shape)");
+    if (o->root_end && o->root_end <= o->root_begin)
+        return fail(MBE_ERR_INVALID_ARG, "root_end must be 0 or greater than root_begin");
+    if (o->reserved0) return fail(MBE_ERR_INVALID_ARG, "mbe_opts.reserved0 must be 0");
+    return MBE_OK;
 }
 
 }  // namespace
@@ -141,8 +154,15 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
     size_t total = 0;
     for (uint32_t i = 0; i < n; i++) total += devs[i]->nR - devs[i]->n_isolated;
     roots.reserve(total);
+    // root sample: positions p = rank - n_isolated of the processing order
+    const uint32_t s_begin = opts ? opts->root_begin : 0u, s_end = opts && opts->root_end ? opts->root_end : ~0u;
+    const uint32_t s_stride = opts && opts->root_stride > 1 ? opts->root_stride : 1u;
     for (uint32_t i = 0; i < n; i++)
-        for (uint32_t r = devs[i]->nR; r-- > devs[i]->n_isolated;) roots.push_back(make_uint2(i, r));
+        for (uint32_t r = devs[i]->nR; r-- > devs[i]->n_isolated;) {
+            const uint32_t p = r - devs[i]->n_isolated;
+            if (p < s_begin || p >= s_end || (p - s_begin) % s_stride) continue;
+            roots.push_back(make_uint2(i, r));
+        }
     if (n > 1)
         std::stable_sort(roots.begin(), roots.end(), [&](const uint2& a, const uint2& b) {
             return devs[a.x]->deg_by_rank[a.y] > devs[b.x]->deg_by_rank[b.y];
@@ -253,7 +273,9 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
                              const mbe_opts* opts, mbe_result* out, float* total_ms) {
     const bool emit = opts && (opts->flags & MBE_OPT_EMIT);
     if (emit && n != 1) return fail(MBE_ERR_INVALID_ARG, "MBE_OPT_EMIT takes one graph (mbe_enumerate)");
-    mbe_status st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    mbe_status st = check_opts(opts);
+    if (st) return st;
+    st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (st) return st;
     std::vector<const DeviceGraph*> devs(n);
     for (uint32_t i = 0; i < n; i++) {

@@ -136,8 +136,13 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     // order of the roots gives the same set of maximal bicliques.
     const uint32_t nR = n_rows, nL = n_cols;
     const uint32_t maxW = (nL + 31) / 32;
+    // Per-block root scratch (u64 words): the root expansion keeps its
+    // count histogram (2 x degree u32) and its Q keep flags (one u32 per
+    // candidate) there once they outgrow shared memory.  A row's degree is
+    // at most n_cols, so n_cols + 1 bounds the first; pow2(n_rows) the second.
     uint32_t keys_cap = 2048;
     while (keys_cap < nR) keys_cap <<= 1;
+    if (keys_cap < nL + 1) keys_cap = nL + 1;
     const uint32_t scr_n = nR < 32 ? 32 : nR;
     uint32_t kc = 32;
     while (kc < scr_n) kc <<= 1;
@@ -234,7 +239,7 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     StaticCtrl hc;
     MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
     MBE_CUDA_TRY(cudaStreamSynchronize(s));
-    if (hc.error == 3) return fail(MBE_ERR_DEVICE_TIMEOUT, "mbe_enumerate_static: a device wait timed out");
+    if (hc.error == kErrTimeout) return fail(MBE_ERR_DEVICE_TIMEOUT, "mbe_enumerate_static: a device wait timed out");
     if (hc.error || hc.n_retry)
         return fail(MBE_ERR_OUT_OF_MEMORY, "mbe_enumerate_static: the search outgrew the static scratch (error " +
                                                std::to_string(hc.error) + ")");

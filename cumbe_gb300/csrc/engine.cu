@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -2272,10 +2273,25 @@ static cudaError_t set_dfs_carveout() {
     return cudaFuncSetAttribute(dfs_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
 }
 
-// The carveout is a hint: if the device refuses it, the default stands and
-// the error it recorded is cleared (it was the last one, so no other is lost).
-static void try_dfs_carveout() {
+// The carveout is a hint, applied once per device (the attribute belongs to
+// the device's context and persists): if the device refuses it, the default
+// stands and only the error the refusal recorded is cleared.  An error that
+// was already pending when this is called (an earlier launch nobody checked)
+// is returned, not swallowed.
+static cudaError_t try_dfs_carveout() {
+    const cudaError_t before = cudaGetLastError();
+    if (before != cudaSuccess) return before;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    constexpr int kMaxDev = 128;
+    static std::mutex mu;
+    static bool done[kMaxDev] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < kMaxDev && done[dev]) return cudaSuccess;
     if (set_dfs_carveout() != cudaSuccess) (void)cudaGetLastError();
+    if (dev >= 0 && dev < kMaxDev) done[dev] = true;
+    return cudaSuccess;
 }
 
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
@@ -2306,7 +2322,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     MBE_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
     int occA = 0, occB = 0;
     MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, expand_roots_kernel, kThreadsA, 0));
-    try_dfs_carveout();
+    MBE_CUDA_TRY(try_dfs_carveout());
     MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occB, dfs_kernel, kThreadsB, 0));
     // root expansion at full occupancy (4 blocks per SM measured 23 -> 15 ms
     // on the 94k x 30k graph against 2), or within the share of the GPU a
@@ -2674,8 +2690,8 @@ cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t
 }
 
 cudaError_t launch_dfs(const EngineArgs& a, unsigned grid, cudaStream_t s) {
-    static const int carved = (try_dfs_carveout(), 0);
-    (void)carved;
+    const cudaError_t e = try_dfs_carveout();
+    if (e != cudaSuccess) return e;
     dfs_kernel<<<grid, kThreadsB, 0, s>>>(a);
     return cudaGetLastError();
 }

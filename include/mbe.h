@@ -112,8 +112,10 @@ typedef struct mbe_opts {
     uint32_t flags;
     uint32_t min_rows;           /* thresholded enumeration: |A| >= min_rows */
     uint32_t min_cols;           /*                          |B| >= min_cols */
-    /* tuning (0 = engine default / autotuned) */
-    uint32_t warps_per_block;
+    /* tuning (0 = engine default) */
+    uint32_t warps_per_block;    /* 0 or MBE_DFS_WARPS_PER_BLOCK: the DFS
+                                    block shape is compiled in; any other
+                                    value returns MBE_ERR_INVALID_ARG      */
     uint32_t blocks_per_sm;
     uint32_t donate_min;         /* min remaining children to donate       */
     uint32_t stack_words;        /* per-warp DFS arena size, 32-bit words  */
@@ -132,7 +134,29 @@ typedef struct mbe_opts {
     uint32_t* emit_nrows;        /* [emit_cap_bicliques] |A| per biclique   */
     uint64_t emit_cap_bicliques;
     uint64_t emit_cap_ids;
+    /* Root sample (all zero = every root).  The reference grabs roots
+     * lowest degree first (src/mbe_cuMBE.cuh:57-64,125-133); here the
+     * processing order is the branching side's vertices with at least one
+     * edge by degree ascending, then id ascending.  Only the roots at
+     * positions p of that order with root_begin <= p < root_end (root_end 0:
+     * no upper bound) and (p - root_begin) % root_stride == 0 (root_stride
+     * 0: 1) are expanded.  A sampled root still excludes every root before
+     * it, so the result covers exactly the maximal bicliques whose
+     * earliest branching-side member is a sampled root.  Used to measure a
+     * fixed share of graphs whose full enumeration is out of reach. */
+    uint32_t root_begin;
+    uint32_t root_end;
+    uint32_t root_stride;
+    uint32_t reserved0;          /* must be 0                              */
+    /* Longest time, in nanoseconds, that a device-side wait of the
+     * enumeration kernels may last while no warp on the device makes
+     * progress; past it the kernels stop and the call returns
+     * MBE_ERR_DEVICE_TIMEOUT, leaving the context usable (0 = 60 s). */
+    uint64_t wait_timeout_ns;
 } mbe_opts;
+
+/* Warps per block of the compiled DFS kernel (mbe_opts.warps_per_block). */
+#define MBE_DFS_WARPS_PER_BLOCK 4u
 
 typedef struct mbe_result {
     uint64_t count;              /* maximal bicliques (thresholds applied)  */

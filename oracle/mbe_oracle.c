@@ -30,7 +30,7 @@
  *
  * Parity pinning: (2) checks (1) on random tiny graphs; (1) is checked on
  * the synthetic workloads against counts printed by the reference's own
- * CUDA_MBE_* kernels (built from its sources by oracle/build_ref.sh and
+ * CUDA_MBE_* kernels (built from its sources by oracle/build_ref.py and
  * driven by oracle/ref_runner.cpp on a GPU).
  *
  * Hash: per biclique h(A,B) = fmix64(SA ^ fmix64(SB + (|A|<<32 | |B|))),
@@ -38,6 +38,7 @@
  * fmix64(b + 0xD1B54A32D192ED03) over cols b; graph hash = sum of h.
  * fmix64 is the splitmix64 output mixer.
  */
+#include <math.h>
 #include <pthread.h>
 #include <stdatomic.h>
 #include <stdint.h>
@@ -161,8 +162,8 @@ typedef struct {
     atomic_int* P_ptr;
     int variant;
     uint32_t min_rows, min_cols;
-    int k_lo;                 /* only roots with ori_P index >= k_lo      */
-    int stride;               /* only every stride-th root (1 = all)       */
+    int p_begin, p_end;       /* root sample: processing positions [p_begin, p_end) ... */
+    int stride;               /* ... every stride-th one from p_begin (1 = all) */
     int last;                 /* index of the first root in processing order */
     oracle_emit* emit;
     /* per-thread ("per-block") state, src/main.cu:72-86 */
@@ -363,12 +364,14 @@ static void* run_block(void* arg) {
         if (lvl == 0) {
             for (;;) {
                 int before = s->P_lp[0];
+                /* a root sample skips roots but keeps their Q semantics:
+                 * the next processed root adds every skipped root to Q.
+                 * Position j = last - k in processing order. */
                 int k = atomic_fetch_sub(s->P_ptr, 1);
-                if (k < s->k_lo) k = -1;
-                /* a stride sample skips roots but keeps their Q semantics:
-                 * the next processed root adds every skipped root to Q */
-                while (k >= 0 && s->stride > 1 && (s->last - k) % s->stride != 0) k = atomic_fetch_sub(s->P_ptr, 1);
-                if (k < s->k_lo) k = -1;
+                while (k >= 0 && s->last - k < s->p_end &&
+                       (s->last - k < s->p_begin || (s->last - k - s->p_begin) % s->stride != 0))
+                    k = atomic_fetch_sub(s->P_ptr, 1);
+                if (k >= 0 && s->last - k >= s->p_end) k = -1;
                 s->P_lp[0] = k;
                 if (k < 0) break;
                 /* Q gains the roots skipped since this block's previous root (:135-150) */
@@ -416,12 +419,15 @@ static int cmp_root(const void* a, const void* b) {
     int x = *(const int*)a, y = *(const int*)b;
     int64_t dx = g_sort_ptr[x + 1] - g_sort_ptr[x], dy = g_sort_ptr[y + 1] - g_sort_ptr[y];
     if (dx != dy) return dx > dy ? -1 : 1; /* degree descending */
-    return x < y ? -1 : x > y;             /* ties: id ascending */
+    return x > y ? -1 : x < y;             /* ties: id descending */
 }
 
 /* ori_P: R ids by degree descending (src/header.cuh:55-63).  The
  * reference's std::sort leaves ties in a libstdc++-defined order; the
- * count does not depend on it, so ties go by id here. */
+ * count does not depend on it, so ties go by id descending here: roots are
+ * processed from the tail, so the processing order is degree ascending,
+ * id ascending, the order the GPU engine ranks roots in (root samples of
+ * the two then cover the same roots). */
 static void ref_order(const ograph* g, int* ori_P) {
     for (int i = 0; i < g->nR; i++) ori_P[i] = i;
     g_sort_ptr = g->rptr;
@@ -489,13 +495,13 @@ static void free_state(ostate* s) {
  * 0 on success, -1 on allocation failure, -2 on emit overflow. */
 static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr, const uint32_t* col_idx,
                               int variant, int n_threads, uint32_t min_rows, uint32_t min_cols, double root_frac,
-                              int stride, oracle_result* out, oracle_emit* emit);
+                              int p_begin, int p_end, int stride, oracle_result* out, oracle_emit* emit);
 
 ORACLE_API int oracle_ref_enumerate(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr,
                                     const uint32_t* col_idx, int variant, int n_threads, uint32_t min_rows,
                                     uint32_t min_cols, double root_frac, oracle_result* out, oracle_emit* emit) {
-    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, min_rows, min_cols, root_frac, 1,
-                              out, emit);
+    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, min_rows, min_cols, root_frac, 0,
+                              -1, 1, out, emit);
 }
 
 /* Bounded sample for timing: only every stride-th root in processing
@@ -505,13 +511,27 @@ ORACLE_API int oracle_ref_enumerate(uint32_t n_rows, uint32_t n_cols, const uint
 ORACLE_API int oracle_ref_enumerate_sampled(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr,
                                             const uint32_t* col_idx, int variant, int n_threads, int stride,
                                             oracle_result* out) {
-    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, 0, 0, 0.0,
+    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, 0, 0, 0.0, 0, -1,
                               stride < 1 ? 1 : stride, out, NULL);
+}
+
+/* Root sample as the GPU engine's mbe_opts takes it: the roots at
+ * processing positions p (degree ascending, id ascending, vertices with
+ * edges only) with p_begin <= p < p_end (p_end < 0: no bound) and
+ * (p - p_begin) % stride == 0.  Each sampled root keeps every earlier root
+ * in its Q, so the result is the maximal bicliques whose earliest member
+ * of the branching side is sampled. */
+ORACLE_API int oracle_ref_enumerate_roots(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr,
+                                          const uint32_t* col_idx, int variant, int n_threads, uint32_t min_rows,
+                                          uint32_t min_cols, int p_begin, int p_end, int stride,
+                                          oracle_result* out) {
+    return ref_enumerate_impl(n_rows, n_cols, row_ptr, col_idx, variant, n_threads, min_rows, min_cols, 0.0,
+                              p_begin < 0 ? 0 : p_begin, p_end, stride < 1 ? 1 : stride, out, NULL);
 }
 
 static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* row_ptr, const uint32_t* col_idx,
                               int variant, int n_threads, uint32_t min_rows, uint32_t min_cols, double root_frac,
-                              int stride, oracle_result* out, oracle_emit* emit) {
+                              int p_begin, int p_end, int stride, oracle_result* out, oracle_emit* emit) {
     memset(out, 0, sizeof *out);
     ograph g;
     ograph_build(&g, n_rows, n_cols, row_ptr, col_idx);
@@ -528,12 +548,11 @@ static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* 
         }
     atomic_int P_ptr;
     atomic_init(&P_ptr, last);
-    int k_lo = 0;
+    if (p_end < 0 || p_end > last + 1) p_end = last + 1;
     if (root_frac > 0.0 && root_frac < 1.0 && last >= 0) {
-        int n = last + 1;
-        int take = (int)(root_frac * n);
-        if (take < 1) take = 1;
-        k_lo = n - take;
+        /* the first root_frac of the roots in processing order */
+        int take = (int)(root_frac * (last + 1));
+        p_end = take < 1 ? 1 : take;
     }
     int rc = 0;
     ostate* st = (ostate*)calloc((size_t)n_threads, sizeof(ostate));
@@ -545,7 +564,8 @@ static int ref_enumerate_impl(uint32_t n_rows, uint32_t n_cols, const uint64_t* 
         st[t].variant = variant;
         st[t].min_rows = min_rows;
         st[t].min_cols = min_cols;
-        st[t].k_lo = k_lo;
+        st[t].p_begin = p_begin;
+        st[t].p_end = p_end;
         st[t].stride = stride;
         st[t].last = last;
         st[t].emit = emit;
@@ -633,3 +653,263 @@ ORACLE_API int oracle_brute(uint32_t n_rows, uint32_t n_cols, const uint64_t* ro
     free(nbr);
     return emit && emit->overflow ? -2 : 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic Chung-Lu generator, restated from the product's generator
+ * (mbe_graph_generate) so that the timed CPU baseline can build its input
+ * without loading the product library.  Same published recipe, same
+ * stream: splitmix64 (Steele, Lea & Flood 2014) seeded by `seed`; weights
+ * w_i = (i+1)^(-1/(gamma-1)) capped at max_deg expected degree by repeated
+ * clipping; endpoints drawn by inverse CDF (first cdf entry above u * total);
+ * duplicates and endpoints at max_deg rejected until n_edges distinct edges
+ * exist or 64 n_edges + 1024 draws were made; then `planted` blocks of
+ * planted_rows x planted_cols at planted_density, half of each side from
+ * the 1% lowest ids (the hubs) and half uniform.  The CSR is sorted by
+ * (row, col).  tests/ checks it equal to the product's on several shapes. */
+
+typedef struct {
+    uint32_t n_rows, n_cols;
+    uint64_t n_edges;
+    double gamma_rows, gamma_cols;
+    uint32_t max_deg;
+    uint64_t seed;
+    uint32_t planted, planted_rows, planted_cols;
+    double planted_density;
+} oracle_gen;
+
+typedef struct {
+    uint64_t s;
+} gen_rng;
+
+static uint64_t gen_next(gen_rng* r) {
+    r->s += 0x9E3779B97F4A7C15ULL;
+    return fmix64(r->s);
+}
+static double gen_u01(gen_rng* r) { return (double)(gen_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+static uint32_t gen_below(gen_rng* r, uint32_t n) {
+    return (uint32_t)(((unsigned __int128)gen_next(r) * n) >> 64);
+}
+
+typedef struct {
+    uint32_t n;
+    int uniform;
+    double* cdf;
+} gen_side;
+
+static int gen_side_build(gen_side* sd, uint32_t n, double gamma, double n_edges, uint32_t cap) {
+    sd->n = n;
+    sd->cdf = NULL;
+    sd->uniform = gamma <= 0.0 || n == 0;
+    if (sd->uniform) return 0;
+    double* w = (double*)malloc(sizeof(double) * n);
+    if (!w) return -1;
+    const double ex = -1.0 / (gamma - 1.0);
+    for (uint32_t i = 0; i < n; i++) w[i] = pow((double)i + 1.0, ex);
+    for (int it = 0; it < 32 && cap; it++) {
+        double tot = 0;
+        for (uint32_t i = 0; i < n; i++) tot += w[i];
+        const double lim = (double)cap * tot / n_edges;
+        int clipped = 0;
+        for (uint32_t i = 0; i < n; i++)
+            if (w[i] > lim * (1 + 1e-12)) {
+                w[i] = lim;
+                clipped = 1;
+            }
+        if (!clipped) break;
+    }
+    double acc = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        acc += w[i];
+        w[i] = acc;
+    }
+    sd->cdf = w;
+    return 0;
+}
+
+static uint32_t gen_side_draw(const gen_side* sd, gen_rng* r) {
+    if (sd->uniform) return gen_below(r, sd->n);
+    const double u = gen_u01(r) * sd->cdf[sd->n - 1];
+    uint32_t lo = 0, hi = sd->n; /* first index with cdf > u */
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (sd->cdf[mid] > u)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo < sd->n ? lo : sd->n - 1;
+}
+
+/* open-addressing set of (row << 32 | col) keys */
+typedef struct {
+    uint64_t* slot;
+    uint64_t mask, used;
+} gen_set;
+
+static int gen_set_init(gen_set* st, uint64_t want) {
+    uint64_t cap = 1024;
+    while (cap < want * 2) cap <<= 1;
+    st->slot = (uint64_t*)malloc(sizeof(uint64_t) * cap);
+    if (!st->slot) return -1;
+    memset(st->slot, 0xFF, sizeof(uint64_t) * cap);
+    st->mask = cap - 1;
+    st->used = 0;
+    return 0;
+}
+
+static int gen_set_insert(gen_set* st, uint64_t key);
+
+static int gen_set_grow(gen_set* st) {
+    uint64_t* old = st->slot;
+    const uint64_t n = st->mask + 1;
+    st->slot = (uint64_t*)malloc(sizeof(uint64_t) * n * 2);
+    if (!st->slot) {
+        st->slot = old;
+        return -1;
+    }
+    memset(st->slot, 0xFF, sizeof(uint64_t) * n * 2);
+    st->mask = n * 2 - 1;
+    st->used = 0;
+    for (uint64_t i = 0; i < n; i++)
+        if (old[i] != ~0ULL) gen_set_insert(st, old[i]);
+    free(old);
+    return 0;
+}
+
+/* 1 = inserted, 0 = present */
+static int gen_set_insert(gen_set* st, uint64_t key) {
+    if ((st->used + 1) * 10 > (st->mask + 1) * 7) gen_set_grow(st);
+    uint64_t h = fmix64(key) & st->mask;
+    for (;;) {
+        if (st->slot[h] == ~0ULL) {
+            st->slot[h] = key;
+            st->used++;
+            return 1;
+        }
+        if (st->slot[h] == key) return 0;
+        h = (h + 1) & st->mask;
+    }
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : x > y;
+}
+
+typedef struct {
+    uint64_t* v;
+    uint64_t n, cap;
+} gen_vec;
+
+static int gen_push(gen_vec* v, uint64_t x) {
+    if (v->n == v->cap) {
+        uint64_t nc = v->cap ? v->cap * 2 : 1024;
+        uint64_t* p = (uint64_t*)realloc(v->v, sizeof(uint64_t) * nc);
+        if (!p) return -1;
+        v->v = p;
+        v->cap = nc;
+    }
+    v->v[v->n++] = x;
+    return 0;
+}
+
+static void gen_pick(gen_rng* r, uint32_t count, uint32_t n, uint32_t hubs, uint32_t* dst, uint32_t* m) {
+    uint32_t tries = 0;
+    *m = 0;
+    while (*m < count && tries < 1000u * count) {
+        tries++;
+        const uint32_t v = ((uint64_t)*m * 2 < count) ? gen_below(r, hubs) : gen_below(r, n);
+        int seen = 0;
+        for (uint32_t i = 0; i < *m; i++)
+            if (dst[i] == v) seen = 1;
+        if (!seen) dst[(*m)++] = v;
+    }
+}
+
+/* Returns 0 and malloc'd arrays row_ptr[n_rows+1], col_idx[*n_edges]
+ * (free with oracle_free), -1 on bad arguments or allocation failure. */
+ORACLE_API int oracle_generate(const oracle_gen* p, uint64_t** row_ptr, uint32_t** col_idx, uint64_t* n_edges) {
+    *row_ptr = NULL;
+    *col_idx = NULL;
+    *n_edges = 0;
+    if ((p->n_rows == 0 || p->n_cols == 0) && p->n_edges) return -1;
+    const uint64_t maxe = (uint64_t)p->n_rows * p->n_cols;
+    const uint64_t target = p->n_edges < maxe ? p->n_edges : maxe;
+    gen_rng rng = {p->seed};
+    gen_side rs, cs;
+    const double te = (double)(target > 1 ? target : 1);
+    if (gen_side_build(&rs, p->n_rows, p->gamma_rows, te, p->max_deg) ||
+        gen_side_build(&cs, p->n_cols, p->gamma_cols, te, p->max_deg))
+        return -1;
+    gen_set set;
+    if (gen_set_init(&set, target + (uint64_t)p->planted * p->planted_rows * p->planted_cols + 16)) return -1;
+    gen_vec keys = {NULL, 0, 0};
+    uint32_t* rdeg = (uint32_t*)calloc((size_t)p->n_rows + 1, sizeof(uint32_t));
+    uint32_t* cdeg = (uint32_t*)calloc((size_t)p->n_cols + 1, sizeof(uint32_t));
+    int rc = (rdeg && cdeg) ? 0 : -1;
+    uint64_t draws = 0;
+    const uint64_t max_draws = 64 * target + 1024;
+    while (rc == 0 && keys.n < target && draws < max_draws) {
+        draws++;
+        const uint32_t r = gen_side_draw(&rs, &rng);
+        const uint32_t c = gen_side_draw(&cs, &rng);
+        if (p->max_deg && (rdeg[r] >= p->max_deg || cdeg[c] >= p->max_deg)) continue;
+        const uint64_t k = ((uint64_t)r << 32) | c;
+        if (gen_set_insert(&set, k)) {
+            rc = gen_push(&keys, k);
+            rdeg[r]++;
+            cdeg[c]++;
+        }
+    }
+    if (rc == 0 && p->planted && p->n_rows && p->n_cols) {
+        const uint32_t hub_r = p->n_rows / 100 ? p->n_rows / 100 : 1, hub_c = p->n_cols / 100 ? p->n_cols / 100 : 1;
+        const uint32_t pr = p->planted_rows < p->n_rows ? p->planted_rows : p->n_rows;
+        const uint32_t pc = p->planted_cols < p->n_cols ? p->planted_cols : p->n_cols;
+        uint32_t* rows = (uint32_t*)malloc(sizeof(uint32_t) * (pr + 1));
+        uint32_t* cols = (uint32_t*)malloc(sizeof(uint32_t) * (pc + 1));
+        if (!rows || !cols) rc = -1;
+        for (uint32_t b = 0; rc == 0 && b < p->planted; b++) {
+            uint32_t nr = 0, nc = 0;
+            gen_pick(&rng, pr, p->n_rows, hub_r, rows, &nr);
+            gen_pick(&rng, pc, p->n_cols, hub_c, cols, &nc);
+            for (uint32_t i = 0; i < nr && rc == 0; i++)
+                for (uint32_t j = 0; j < nc && rc == 0; j++)
+                    if (gen_u01(&rng) < p->planted_density) {
+                        const uint64_t k = ((uint64_t)rows[i] << 32) | cols[j];
+                        if (gen_set_insert(&set, k)) rc = gen_push(&keys, k);
+                    }
+        }
+        free(rows);
+        free(cols);
+    }
+    free(rdeg);
+    free(cdeg);
+    free(set.slot);
+    free(rs.cdf);
+    free(cs.cdf);
+    if (rc) {
+        free(keys.v);
+        return -1;
+    }
+    qsort(keys.v, keys.n, sizeof(uint64_t), cmp_u64);
+    uint64_t* rp = (uint64_t*)calloc((size_t)p->n_rows + 1, sizeof(uint64_t));
+    uint32_t* ci = (uint32_t*)malloc(sizeof(uint32_t) * (keys.n ? keys.n : 1));
+    if (!rp || !ci) {
+        free(rp);
+        free(ci);
+        free(keys.v);
+        return -1;
+    }
+    for (uint64_t i = 0; i < keys.n; i++) {
+        rp[(keys.v[i] >> 32) + 1]++;
+        ci[i] = (uint32_t)keys.v[i];
+    }
+    for (uint32_t r = 0; r < p->n_rows; r++) rp[r + 1] += rp[r];
+    free(keys.v);
+    *row_ptr = rp;
+    *col_idx = ci;
+    *n_edges = rp[p->n_rows];
+    return 0;
+}
+
+ORACLE_API void oracle_free(void* ptr) { free(ptr); }

@@ -25,6 +25,13 @@ class _Result(ctypes.Structure):
                 ("nodes", ctypes.c_uint64), ("scanned", ctypes.c_uint64)]
 
 
+class _Gen(ctypes.Structure):
+    _fields_ = [("n_rows", ctypes.c_uint32), ("n_cols", ctypes.c_uint32), ("n_edges", ctypes.c_uint64),
+                ("gamma_rows", ctypes.c_double), ("gamma_cols", ctypes.c_double), ("max_deg", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64), ("planted", ctypes.c_uint32), ("planted_rows", ctypes.c_uint32),
+                ("planted_cols", ctypes.c_uint32), ("planted_density", ctypes.c_double)]
+
+
 class _Emit(ctypes.Structure):
     _fields_ = [("cap_bicliques", ctypes.c_uint64), ("cap_ids", ctypes.c_uint64),
                 ("n_bicliques", ctypes.c_uint64), ("n_ids", ctypes.c_uint64),
@@ -47,7 +54,7 @@ def build(force: bool = False) -> str:
     """Compiles liboracle.so with gcc (portable flags: x86 and Arm)."""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC_PATH):
         subprocess.check_call(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread",
-                               "-fvisibility=hidden", SRC_PATH, "-o", LIB_PATH + ".tmp"])
+                               "-fvisibility=hidden", SRC_PATH, "-o", LIB_PATH + ".tmp", "-lm"])
         os.replace(LIB_PATH + ".tmp", LIB_PATH)
     return LIB_PATH
 
@@ -69,6 +76,15 @@ def lib():
         L.oracle_ref_enumerate_sampled.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u64p, u32p, ctypes.c_int,
                                                    ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Result)]
         L.oracle_ref_enumerate_sampled.restype = ctypes.c_int
+        L.oracle_ref_enumerate_roots.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u64p, u32p, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Result)]
+        L.oracle_ref_enumerate_roots.restype = ctypes.c_int
+        L.oracle_generate.argtypes = [ctypes.POINTER(_Gen), ctypes.POINTER(u64p), ctypes.POINTER(u32p),
+                                      ctypes.POINTER(ctypes.c_uint64)]
+        L.oracle_generate.restype = ctypes.c_int
+        L.oracle_free.argtypes = [ctypes.c_void_p]
+        L.oracle_free.restype = None
         L.oracle_brute.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u64p, u32p, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.POINTER(_Result), ctypes.POINTER(_Emit)]
         L.oracle_brute.restype = ctypes.c_int
@@ -133,6 +149,42 @@ def ref_enumerate_sampled(n_rows, n_cols, row_ptr, col_idx, stride, variant="cuM
     if rc != 0:
         raise RuntimeError(f"oracle_ref_enumerate_sampled failed rc={rc}")
     return OracleResult(res.count, res.hash, res.nodes, res.scanned)
+
+
+def ref_enumerate_roots(n_rows, n_cols, row_ptr, col_idx, root_begin=0, root_end=0, root_stride=1,
+                        variant="cuMBE", threads=1, min_rows=0, min_cols=0) -> OracleResult:
+    """The restatement over a root sample: processing positions p (degree
+    ascending, id ascending, vertices with edges only) with root_begin <= p
+    < root_end (0: no bound) and (p - root_begin) % root_stride == 0; the
+    same sample mbe_opts.root_begin/root_end/root_stride selects."""
+    rp, ci, prp, pci = _ptrs(row_ptr, col_idx)
+    res = _Result()
+    rc = lib().oracle_ref_enumerate_roots(n_rows, n_cols, prp, pci, VARIANTS[variant], threads, min_rows,
+                                          min_cols, root_begin, root_end if root_end else -1, max(1, root_stride),
+                                          ctypes.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"oracle_ref_enumerate_roots failed rc={rc}")
+    return OracleResult(res.count, res.hash, res.nodes, res.scanned)
+
+
+def generate(n_rows, n_cols, n_edges, gamma_rows=2.1, gamma_cols=2.1, max_deg=0, seed=1, planted=0,
+             planted_rows=0, planted_cols=0, planted_density=0.0):
+    """The synthetic generator restated in the oracle (same graph as
+    cumbe_gb300.Graph.generate): returns (n_rows, n_cols, row_ptr, col_idx)."""
+    p = _Gen(n_rows, n_cols, n_edges, gamma_rows, gamma_cols, max_deg, seed, planted, planted_rows, planted_cols,
+             planted_density)
+    rp = ctypes.POINTER(ctypes.c_uint64)()
+    ci = ctypes.POINTER(ctypes.c_uint32)()
+    ne = ctypes.c_uint64()
+    if lib().oracle_generate(ctypes.byref(p), ctypes.byref(rp), ctypes.byref(ci), ctypes.byref(ne)) != 0:
+        raise RuntimeError("oracle_generate failed")
+    try:
+        row_ptr = np.ctypeslib.as_array(rp, shape=(n_rows + 1,)).copy()
+        col_idx = np.ctypeslib.as_array(ci, shape=(max(1, ne.value),))[:ne.value].copy()
+    finally:
+        lib().oracle_free(ctypes.cast(rp, ctypes.c_void_p))
+        lib().oracle_free(ctypes.cast(ci, ctypes.c_void_p))
+    return n_rows, n_cols, row_ptr, col_idx
 
 
 def brute(n_rows, n_cols, row_ptr, col_idx, min_rows=0, min_cols=0, emit_cap=0) -> OracleResult:

@@ -1,0 +1,83 @@
+"""GPU: root samples and bounded device waits, through the C ABI.
+
+Root samples (mbe_opts.root_begin / root_end / root_stride) select roots by
+their position in the processing order (degree ascending, id ascending);
+the engine's result must equal the oracle's over the same sample, and
+disjoint samples must add up to the whole graph's count and hash.
+
+The bounded waits: every device-side wait of the enumeration kernels ends,
+after wait_timeout_ns without progress anywhere on the device, in an error
+status the host reads (MBE_ERR_DEVICE_TIMEOUT), never a trap.  A limit of
+1 ns makes the idle warps' waits for a task run out; the call must fail
+with that status, the kernels must have exited, and the same context must
+then enumerate correctly."""
+import numpy as np
+import pytest
+
+import cumbe_gb300 as cm
+import oracle
+from conftest import random_csr
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs():
+    rng = np.random.default_rng(77)
+    return {
+        "power_law_2k_1k": cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1).csr(),  # rows > cols: swapped
+        "random_90x160": random_csr(rng, 90, 160, 0.08),                                # not swapped
+    }
+
+
+SAMPLES = [dict(root_begin=0, root_stride=3), dict(root_begin=1, root_stride=3), dict(root_begin=2, root_stride=3),
+           dict(root_begin=100, root_end=700), dict(root_begin=5, root_stride=7), dict(root_begin=0, root_end=1)]
+
+
+@pytest.mark.parametrize("name", ["power_law_2k_1k", "random_90x160"])
+@pytest.mark.parametrize("variant", ["cuMBE", "noWS"])
+def test_root_sample_matches_oracle(engine, name, variant):
+    nr, nc, rp, ci = _graphs()[name]
+    G = cm.Graph.from_csr(nr, nc, rp, ci)
+    for smp in SAMPLES:
+        want = oracle.ref_enumerate_roots(nr, nc, rp, ci, variant=variant, threads=4, **smp)
+        got = engine.enumerate(G, variant, **smp)
+        assert (got.count, got.hash) == (want.count, want.hash), (name, variant, smp)
+
+
+def test_disjoint_samples_add_up_to_the_whole_graph(engine):
+    nr, nc, rp, ci = _graphs()["power_law_2k_1k"]
+    G = cm.Graph.from_csr(nr, nc, rp, ci)
+    full = engine.enumerate(G)
+    parts = [engine.enumerate(G, root_begin=k, root_stride=4) for k in range(4)]
+    assert sum(p.count for p in parts) == full.count
+    assert sum(p.hash for p in parts) % (1 << 64) == full.hash
+
+
+def test_root_sample_in_a_batch(engine):
+    gs = [cm.Graph.generate(**p) for p in
+          [dict(n_rows=300, n_cols=150, n_edges=2500, seed=s, gamma_rows=0.0, gamma_cols=0.0) for s in range(6)]]
+    res, _ = engine.batch(gs, root_begin=3, root_stride=2)
+    for g, r in zip(gs, res):
+        want = oracle.ref_enumerate_roots(*g.csr(), root_begin=3, root_stride=2, threads=4)
+        assert (r.count, r.hash) == (want.count, want.hash)
+
+
+def test_bad_options_are_rejected(engine):
+    G = cm.Graph.generate(200, 100, 800, 2.1, 2.1, 0, 1)
+    for bad in [dict(warps_per_block=3), dict(root_begin=10, root_end=10)]:
+        with pytest.raises(cm.MBEError) as e:
+            engine.enumerate(G, **bad)
+        assert e.value.status == 1  # MBE_ERR_INVALID_ARG
+    engine.enumerate(G, warps_per_block=4)  # the compiled shape is accepted
+
+
+def test_device_wait_timeout_is_an_error_status_and_the_context_recovers(engine):
+    g = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    want = oracle.ref_enumerate(*g.csr(), threads=4)
+    with pytest.raises(cm.MBEError) as e:
+        engine.enumerate(g, wait_timeout_ns=1)
+    assert e.value.status == 6  # MBE_ERR_DEVICE_TIMEOUT
+    assert "timed out" in str(e.value)
+    for _ in range(2):
+        got = engine.enumerate(g)
+        assert (got.count, got.hash) == (want.count, want.hash)

@@ -62,3 +62,30 @@ def test_hash_is_order_free(built):
     h2 = oracle.biclique_hash([1, 2, 3], [7, 9])
     assert h1 == h2
     assert h1 != oracle.biclique_hash([7, 9], [1, 2, 3])
+
+
+def test_oracle_generator_matches_the_library(built):
+    """The oracle's restatement of the synthetic generator (used by the
+    CPU baseline, which must not load the product library) builds the same
+    graph as mbe_graph_generate: Chung-Lu, capped, uniform and planted."""
+    import cumbe_gb300 as cm
+    from cumbe_gb300 import workloads
+    cases = [workloads.SINGLE["power_law_2k_1k"], workloads.SINGLE["power_law_94k_30k"],
+             dict(n_rows=28000, n_cols=10000, n_edges=160000, gamma_rows=1.9, gamma_cols=1.9, max_deg=0, seed=3,
+                  planted=4, planted_rows=20, planted_cols=30, planted_density=0.9)] + workloads.batch(6)
+    for p in cases:
+        a = oracle.generate(**p)
+        b = cm.Graph.generate(**p).csr()
+        assert a[:2] == b[:2]
+        assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3]), p
+
+
+def test_root_samples_partition_the_roots(built):
+    csr = oracle.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    full = oracle.ref_enumerate(*csr, threads=4)
+    parts = [oracle.ref_enumerate_roots(*csr, root_begin=k, root_stride=3, threads=4) for k in range(3)]
+    assert sum(p.count for p in parts) == full.count
+    assert sum(p.hash for p in parts) % (1 << 64) == full.hash
+    lo = oracle.ref_enumerate_roots(*csr, root_end=400, threads=4)
+    hi = oracle.ref_enumerate_roots(*csr, root_begin=400, threads=4)
+    assert (lo.count + hi.count, (lo.hash + hi.hash) % (1 << 64)) == (full.count, full.hash)

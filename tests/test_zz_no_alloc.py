@@ -6,13 +6,14 @@ that cannot afford the synchronisation of cudaMalloc/cudaFree, plugin
 runtimes without an allocation budget).  The test allocates the graph and
 result buffers itself (with torch), calls the entry point through the C ABI
 twice in a row, and checks count and canonical hash bit-exactly against
-mbe_enumerate on the same graph.  Collected last so that a failure here
+mbe_enumerate and the CPU oracle on the same graph.  Collected last so that a failure here
 stops a -x run only after every other test has run.
 """
 import numpy as np
 import pytest
 
 import cumbe_gb300 as cm
+import oracle
 from conftest import random_csr
 
 pytestmark = pytest.mark.gpu
@@ -54,8 +55,50 @@ def test_static_matches_enumerate_twice(engine, case):
         g = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1).csr()
     nr, nc, rp, ci = g
     want = engine.enumerate(cm.Graph.from_csr(nr, nc, rp, ci))
+    ref = oracle.ref_enumerate(nr, nc, rp, ci, threads=4)
+    assert (want.count, want.hash) == (ref.count, ref.hash)
     bufs = _device_csr(nr, nc, rp, ci)
     for _ in range(2):  # the second call reuses the array the first one left behind
+        assert _call_static(nr, nc, bufs) == (want.count, want.hash)
+
+
+def _wide_row_csr(rng, nr=100, nc=3000, wide_deg=2600, p=0.05):
+    """Row 0 meets wide_deg of the nc cols (a root whose degree needs more
+    than the 4,096 u32 of shared histogram: 2 x degree > 4096); the other
+    rows are uniform at density p, so row 0's root has candidates of higher
+    id (a non-empty P side) and of lower id (none: it is row 0) alike."""
+    M = rng.random((nr, nc)) < p
+    M[0, :] = False
+    M[0, rng.choice(nc, wide_deg, replace=False)] = True
+    rp = np.zeros(nr + 1, np.uint64)
+    rp[1:] = np.cumsum(M.sum(1))
+    return nr, nc, rp, np.nonzero(M)[1].astype(np.uint32)
+
+
+@pytest.mark.parametrize("wide_row", [0, 57])
+def test_static_row_wider_than_shared_histogram(engine, wide_row):
+    """A row of degree 2,600 of 3,000 cols: its root expansion keeps the
+    count histogram in the per-block global scratch, which must be sized
+    for the widest row.  Count and hash bit-exact against the oracle and
+    against mbe_enumerate, on two calls in a row."""
+    rng = np.random.default_rng(5 + wide_row)
+    nr, nc, rp, ci = _wide_row_csr(rng)
+    if wide_row:
+        # move the wide row to position wide_row: its root then has both a Q
+        # (rows below it) and a P (rows above it) side
+        order = np.r_[np.arange(1, wide_row + 1), 0, np.arange(wide_row + 1, nr)]
+        deg = np.diff(rp.astype(np.int64))
+        rows = [ci[rp[r]:rp[r + 1]] for r in range(nr)]
+        rows = [rows[r] for r in order]
+        rp = np.zeros(nr + 1, np.uint64)
+        rp[1:] = np.cumsum([len(x) for x in rows])
+        ci = np.concatenate(rows).astype(np.uint32)
+        assert deg.max() == 2600
+    want = oracle.ref_enumerate(nr, nc, rp, ci, threads=4)
+    got = engine.enumerate(cm.Graph.from_csr(nr, nc, rp, ci))
+    assert (got.count, got.hash) == (want.count, want.hash)
+    bufs = _device_csr(nr, nc, rp, ci)
+    for _ in range(2):
         assert _call_static(nr, nc, bufs) == (want.count, want.hash)
 
 
