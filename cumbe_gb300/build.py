@@ -37,7 +37,7 @@ def _flags() -> list[str]:
     if os.environ.get("MBE_PROFILE") == "1":
         f += ["-DMBE_PROFILE"]
     # MBE_DFS_BLOCKS=N sets the resident blocks per SM the enumeration kernel
-    # is compiled for (its register budget); default 5.
+    # is compiled for (its register budget); default 6.
     if os.environ.get("MBE_DFS_BLOCKS"):
         f += ["-DMBE_DFS_MIN_BLOCKS=%d" % int(os.environ["MBE_DFS_BLOCKS"])]
     # MBE_UNROLL=E,G,P sets the scan unroll factors of the enumeration kernel
@@ -45,7 +45,7 @@ def _flags() -> list[str]:
     # MBE_DFS_WARPS=N sets its warps per block; default 4.
     if os.environ.get("MBE_DFS_WARPS"):
         f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]
-    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX"):  # tuning sweeps
+    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX", "MBE_SMEM_W", "MBE_SH_ROWS"):  # tuning sweeps
         if os.environ.get(knob):
             f += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if os.environ.get("MBE_EVAL_NOINLINE") == "1":

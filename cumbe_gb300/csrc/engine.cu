@@ -35,7 +35,15 @@ namespace {
 constexpr int kThreadsA = 256;
 constexpr int kWarpsB = kDfsWarps;
 constexpr int kThreadsB = kWarpsB * 32;
-constexpr uint32_t kSmemW = 64;          // Li words cached in shared memory per warp
+// Shared-memory sizes per DFS warp, chosen so that MBE_DFS_MIN_BLOCKS
+// blocks fit the 64 KB carveout (the rest of the SM's memory stays L1).
+#ifndef MBE_SMEM_W
+#define MBE_SMEM_W 32
+#endif
+#ifndef MBE_SH_ROWS
+#define MBE_SH_ROWS 40
+#endif
+constexpr uint32_t kSmemW = MBE_SMEM_W;  // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
 #ifndef MBE_KEEP_WINDOW
 #define MBE_KEEP_WINDOW 32
@@ -45,7 +53,7 @@ constexpr unsigned long long kInvalidKey = ~0ull;
 #endif
 constexpr uint32_t kKeepWindow = MBE_KEEP_WINDOW;  // Q rows a dropped Q row is tested against (<= 32)
 constexpr unsigned kPopSleepMax = MBE_POP_SLEEP_MAX;  // ns, back-off ceiling of a warp waiting for a task
-constexpr uint32_t kShRows = 64;         // Q' rows / P' keys of a packed build kept in shared memory
+constexpr uint32_t kShRows = MBE_SH_ROWS;  // Q' rows / P' keys of a packed build kept in shared memory
 #ifndef MBE_UNROLL_E
 #define MBE_UNROLL_E 1
 #endif
@@ -131,8 +139,8 @@ __device__ bool push_task(const EngineArgs& a, Task t) {
             pa_t = t__;                                                                 \
         }                                                                               \
     } while (0)
-#define PROF_VAL(acc_arr, sec, v) do { (acc_arr)[2 * (sec)] += (v); (acc_arr)[2 * (sec) + 1]++; } while (0)
-#define PROF_ADD(acc_arr, sec) do { (acc_arr)[2 * (sec)] += clock64() - prof_t0__; (acc_arr)[2 * (sec) + 1]++; prof_t0__ = clock64(); } while (0)
+#define PROF_VAL(acc_arr, sec, v) do { if (lane_id() == 0) { (acc_arr)[2 * (sec)] += (v); (acc_arr)[2 * (sec) + 1]++; } } while (0)
+#define PROF_ADD(acc_arr, sec) do { const long long t__ = clock64(); if (lane_id() == 0) { (acc_arr)[2 * (sec)] += t__ - prof_t0__; (acc_arr)[2 * (sec) + 1]++; } prof_t0__ = clock64(); } while (0)
 #else
 #define PROF_T0() do {} while (0)
 #define PROF_ADD(acc_arr, sec) do {} while (0)
@@ -307,7 +315,7 @@ __device__ void root_rlist(uint32_t x, const uint32_t* cl, const uint32_t* cntA,
 // ---------------------------------------------------------------------------
 // Phase A: root expansion
 
-__global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
+__global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_constant__ EngineArgs a) {
     __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax, s_counted;
     __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
     __shared__ unsigned long long s_sabs, s_sl, s_rec, s_scan;
@@ -724,32 +732,44 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(EngineArgs a) {
 // ---------------------------------------------------------------------------
 // Phase B: warp DFS with donation
 
+// Per-warp state of the DFS kernel.  It is warp-uniform, so it lives in
+// shared memory, one copy per warp: kept in local memory it would be held
+// once per lane (local memory is per thread) and compete with the record
+// scans for L1.  Lane 0 writes it (at kernel start, and slab_* when
+// donating); every lane reads it.
 struct WarpCtx {
-    uint32_t* arena;
-    uint32_t arena_top;
+    uint32_t* arena;       // this warp's DFS arena (a.arena_words words)
     uint32_t* scrLi;
     uint32_t* scrNz;
     uint32_t* scrQcnt;
     unsigned long long* scrKeysP;
     unsigned long long* scrKeysQ;
-    uint32_t* sLi;
-    uint32_t* sNz;
     uint32_t* scrPack;     // 2 x kc words: srow, spos of a packed build too large for shared memory
     uint32_t* scrHist;     // 32 maxW + 32 words: count histogram of a wide child's sorts
     uint32_t* scrAbs;      // scr_n words: ranks absorbed by the child being evaluated (output stream only)
     uint32_t scr_kc;       // key-array capacity of this launch's scratch layout
-    uint32_t* sBucket;     // 64 words of shared memory: Q' then P' count buckets
-    uint32_t* shRow;       // kShRows Q' rows of a packed build (shared memory)
-    uint32_t* shPos;       // their parent positions
-    unsigned long long* shKeys;  // kShRows P' keys of a packed child (shared memory)
-    SolveLevel* solve;     // kSolveRows + 1 saved levels (shared memory)
     unsigned long long slab_off, slab_end;  // this warp's slab of the node pool (donation copies)
 #ifdef MBE_PROFILE
-    long long prof[kProfSlots];
+    long long prof[kProfSlots];    // section cycles and events (lane 0 adds)
     unsigned long long last_busy;  // globaltimer when the warp last finished a task
     unsigned long long t_start;    // globaltimer at kernel start
 #endif
 };
+
+// Shared memory of the DFS kernel, per warp (file scope, so that the
+// out-of-line helpers address it directly).
+__shared__ WarpCtx s_wc[kWarpsB];
+__shared__ uint32_t s_Li[kWarpsB][kSmemW];        // L_i words (when W <= kSmemW)
+__shared__ uint32_t s_Nz[kWarpsB][kSmemW];        // their record word indices
+__shared__ uint32_t s_Bucket[kWarpsB][64];        // Q' then P' count buckets of a packed build
+__shared__ uint32_t s_Row[kWarpsB][kShRows];      // Q' rows of a packed build
+__shared__ uint32_t s_Pos[kWarpsB][kShRows];      // their parent positions
+__shared__ unsigned long long s_Keys[kWarpsB][kShRows];  // P' keys of a packed child
+__shared__ SolveLevel s_Solve[kWarpsB][kSolveRows + 1];  // saved levels of the register search
+__shared__ GraphView s_G[kWarpsB];                // the graph of the warp's current task
+
+__device__ __forceinline__ uint32_t warp_in_block() { return threadIdx.x >> 5; }
+__device__ __forceinline__ WarpCtx& my_wc() { return s_wc[warp_in_block()]; }
 
 // Ticket queue: an idle warp takes the next slot index with one atomicAdd
 // and then watches only that slot's ready flag, so waiting warps never
@@ -757,8 +777,15 @@ struct WarpCtx {
 // ends when the slot is ready, or when pending == 0 (no queued and no
 // running task: nothing can be pushed any more), or on an error, or when
 // no warp has made progress for timeout_ns.
-__device__ __noinline__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my_path) {
+struct Popped {
+    unsigned long long node;   // 0 when no task was taken (done, error)
+    uint32_t begin, end, plen;
+    uint32_t path;             // lane j holds path[j]
+};
+
+__device__ __noinline__ Popped pop_task(const EngineArgs& a) {
     unsigned lane = lane_id();
+    Popped t{0ull, 0u, 0u, 0u, 0u};
     int state = 0;  // 1 = got, 2 = done
     uint32_t h = 0;
     if (lane == 0) {
@@ -793,27 +820,28 @@ __device__ __noinline__ bool pop_task(const EngineArgs& a, Task& t, uint32_t& my
     }
     state = __shfl_sync(kFull, state, 0);
     h = __shfl_sync(kFull, h, 0);
-    if (state != 1) return false;
+    if (state != 1) return t;
     const uint32_t slot = h % a.task_cap;
     volatile Task* src = (volatile Task*)&a.tasks[slot];
     t.node = src->node;
     t.begin = src->begin;
     t.end = src->end;
     t.plen = src->plen;
-    my_path = lane < t.plen ? src->path[lane] : 0u;  // lane j holds path[j]
+    t.path = lane < t.plen ? src->path[lane] : 0u;
     __syncwarp();
     if (lane == 0) {
         __threadfence();
         atomicExch(&a.ready[slot], 0u);
         atomicAdd(a.q_done, 1u);
     }
-    return true;
+    return t;
 }
 
 struct ChildOut {
     uint32_t* rec;
     uint32_t nchild;
     uint32_t size;   // words taken from the arena (0 when in the pool)
+    unsigned long long words;  // set words the out-of-line wide build streamed (added by its caller)
 };
 
 
@@ -1022,17 +1050,19 @@ __device__ __forceinline__ uint32_t bucket_offsets(uint32_t* sb) {
 __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const NodeHdr* h, uint32_t xi, uint32_t li,
                                  uint32_t nnz, const uint32_t* Li, const uint32_t* Nz, uint32_t npp, uint32_t nR2,
                                  unsigned long long sR2, const unsigned long long* keysP, const GraphView& G,
-                                 WarpCtx& wc, ResultAcc& acc) {
+                                 uint32_t arena_top, ResultAcc& acc) {
     const unsigned lane = lane_id();
+    const uint32_t wb = warp_in_block();
+    WarpCtx& wc = my_wc();
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t* M = R.M;
     const CompressPlan plan0 = compress_plan(Li[0]);
     const uint32_t* M0 = M + (size_t)Nz[0] * n;
-    ChildOut out{nullptr, 0, 0};
+    ChildOut out{nullptr, 0, 0, 0ull};
     PROF_T0();
     // Q' = rows of Q u P[0..i) meeting L_i, by count descending (key li -
     // count in 1..31), parent order within a count
-    uint32_t* sb = wc.sBucket;
+    uint32_t* sb = s_Bucket[wb];
     sb[lane] = 0;
     __syncwarp();
     for (uint32_t base = 0; base < xi; base += 32 * kUnrollG) {  // kUnrollG chunks per step: independent loads
@@ -1052,8 +1082,8 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     }
     const uint32_t m = bucket_offsets(sb);
     const bool shq = m <= kShRows;
-    uint32_t* srow = shq ? wc.shRow : wc.scrPack;
-    uint32_t* spos = shq ? wc.shPos : wc.scrPack + wc.scr_kc;
+    uint32_t* srow = shq ? s_Row[wb] : wc.scrPack;
+    uint32_t* spos = shq ? s_Pos[wb] : wc.scrPack + wc.scr_kc;
     for (uint32_t base = 0; base < xi; base += 32 * kUnrollG) {
         uint32_t r[kUnrollG];
 #pragma unroll
@@ -1123,14 +1153,14 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     }
     PROF_ADD(wc.prof, kProfBReduce);
     // P' by count ascending, parent order within a count (keys in scan order)
-    uint32_t* sbp = wc.sBucket + 32;
+    uint32_t* sbp = s_Bucket[wb] + 32;
     bucket_offsets(sbp);
     // allocate and write
     const uint32_t n2 = nq2 + npp;
     const uint64_t rw = a.emit ? record_words_r(1, n2, true, nR2) : record_words(1, n2, true);
     uint32_t* rec;
-    if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
-        rec = wc.arena + wc.arena_top;
+    if ((uint64_t)arena_top + rw <= a.arena_words) {
+        rec = wc.arena + arena_top;
         out.size = (uint32_t)rw;
     } else {
         unsigned long long off = 0;
@@ -1273,15 +1303,17 @@ __device__ void warp_count_sort(unsigned long long* keys, uint32_t n, uint32_t B
 __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
                                                uint32_t xi, uint32_t li, uint32_t nnz, const uint32_t* Li,
                                                const uint32_t* Nz, uint32_t npp, uint32_t nR2,
-                                               unsigned long long sR2, bool known_max, WarpCtx& wc, ResultAcc& acc) {
+                                               unsigned long long sR2, bool known_max, uint32_t arena_top) {
     const unsigned lane = lane_id();
+    WarpCtx& wc = my_wc();
+    struct { unsigned long long words; } acc{0ull};  // set words streamed, returned in ChildOut
     PROF_T0();
     const NodeHdr* h = (const NodeHdr*)nd;
     const RecView R = rec_view(nd);
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t* M = R.M;
     const uint32_t* cand = R.cand;
-    ChildOut out{nullptr, 0, 0};
+    ChildOut out{nullptr, 0, 0, 0ull};
     if (known_max) {
         // the prefilter only settled maximality: count Q u P[0..i) now
         for (uint32_t base = 0; base < xi; base += 32) {
@@ -1362,8 +1394,8 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
     const uint32_t n2 = nq2 + npp, W2 = nnz;  // |L_i| > 32 here: an unpacked child
     const uint64_t rw = a.emit ? record_words_r(W2, n2, false, nR2) : record_words(W2, n2, false);
     uint32_t* rec;
-    if ((uint64_t)wc.arena_top + rw <= a.arena_words) {
-        rec = wc.arena + wc.arena_top;
+    if ((uint64_t)arena_top + rw <= a.arena_words) {
+        rec = wc.arena + arena_top;
         out.size = (uint32_t)rw;
     } else {
         unsigned long long off = 0;
@@ -1372,7 +1404,10 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
             if (off == ~0ull) set_error(a, kErrPool, rw);
         }
         off = __shfl_sync(kFull, off, 0);
-        if (off == ~0ull) return out;
+        if (off == ~0ull) {
+            out.words = acc.words;
+            return out;
+        }
         rec = a.pool + off;
         out.size = 0;
     }
@@ -1421,6 +1456,7 @@ __device__ __noinline__ ChildOut build_general(const EngineArgs& a, const GraphV
     PROF_ADD(wc.prof, kProfBuild);
     out.rec = rec;
     out.nchild = npp;
+    out.words = acc.words;
     return out;
 }
 
@@ -1440,13 +1476,15 @@ __device__ __noinline__
 #else
 __device__
 #endif
-ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, WarpCtx& wc,
+ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, uint32_t arena_top,
                                ResultAcc& acc_out, bool replay, bool known_max) {
     // a replayed evaluation re-derives a donated node: its counts belong to
     // the donor and are discarded
     ResultAcc scratch_acc{};
     ResultAcc& acc = replay ? scratch_acc : acc_out;
     const unsigned lane = lane_id();
+    const uint32_t wb = warp_in_block();
+    WarpCtx& wc = my_wc();
     PROF_T0();
     const NodeHdr* h = (const NodeHdr*)nd;
     const RecView R = rec_view(nd);
@@ -1456,9 +1494,9 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
     const uint32_t* cand = R.cand;
     const uint32_t xi = nq + i;
     const uint32_t li = R.cnt[xi];
-    uint32_t* Li = W <= kSmemW ? wc.sLi : wc.scrLi;
-    uint32_t* Nz = W <= kSmemW ? wc.sNz : wc.scrNz;
-    ChildOut out{nullptr, 0, 0};
+    uint32_t* Li = W <= kSmemW ? s_Li[wb] : wc.scrLi;
+    uint32_t* Nz = W <= kSmemW ? s_Nz[wb] : wc.scrNz;
+    ChildOut out{nullptr, 0, 0, 0ull};
 
     // 1. L_i = L n N(x_i), keeping only non-zero words
     uint32_t nnz = 0;
@@ -1512,8 +1550,8 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
     // For a packed child (|L_i| <= 32) the P' count histogram is taken here
     // and the keys stay in shared memory when they fit.
     const bool packed_child = li <= 32;
-    unsigned long long* keysP = packed_child && n - xi - 1 <= kShRows ? wc.shKeys : wc.scrKeysP;
-    if (packed_child) wc.sBucket[32 + lane] = 0;
+    unsigned long long* keysP = packed_child && n - xi - 1 <= kShRows ? s_Keys[wb] : wc.scrKeysP;
+    if (packed_child) s_Bucket[wb][32 + lane] = 0;
     __syncwarp();
     uint32_t npp = 0, nabs = 0;
     unsigned long long sabs = 0;
@@ -1545,7 +1583,7 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
             if (a.emit && absorbed) wc.scrAbs[nabs + __popc(ab & lanemask_lt())] = cand[c];
             if (packed_child && pb) {
                 unsigned grp = __match_any_sync(kFull, partial ? cc : 32u);
-                if (partial && (grp & lanemask_lt()) == 0) atomicAdd(&wc.sBucket[32 + cc], (uint32_t)__popc(grp));
+                if (partial && (grp & lanemask_lt()) == 0) atomicAdd(&s_Bucket[wb][32 + cc], (uint32_t)__popc(grp));
             }
             npp += __popc(pb);
             nabs += __popc(ab);
@@ -1583,14 +1621,15 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
     PROF_ADD(wc.prof, kProfExpand);
     if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
     if (packed_child) {
-        out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, keysP, G, wc, acc);
+        out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, keysP, G, arena_top, acc);
         PROF_ADD(wc.prof, kProfBuild);
         return out;
     }
 #ifdef MBE_PROFILE
     const long long c0g = clock64();
 #endif
-    out = build_general(a, G, nd, xi, li, nnz, Li, Nz, npp, nR2, sR2, known_max, wc, acc);
+    out = build_general(a, G, nd, xi, li, nnz, Li, Nz, npp, nR2, sR2, known_max, arena_top);
+    acc.words += out.words;
 #ifdef MBE_PROFILE
     PROF_VAL(wc.prof, kProfGeneral, clock64() - c0g);
 #endif
@@ -1673,9 +1712,9 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, R
 // allocation) and shared by pointer; otherwise it is described by the
 // child-index path from frame 0 (always a pool record), which each receiver
 // replays.  Warp-collective.
-__device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int depth, WarpCtx& wc,
-                                        uint32_t waiters) {
+__device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int depth, uint32_t waiters) {
     unsigned lane = lane_id();
+    WarpCtx& wc = my_wc();
     int k = -1;
     for (int base = 0; base <= depth && k < 0; base += 32) {
         int f = base + (int)lane;
@@ -1709,20 +1748,27 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
         const unsigned long long need = (words + 31ull) & ~31ull;  // whole 128-byte lines
         const unsigned long long limit = a.pool_words / 10 * 6;
         if (words <= kDonateSlabMax) {
-            if (wc.slab_off + need > wc.slab_end) {
+            unsigned long long so = wc.slab_off, se = wc.slab_end;  // the warp's slab (uniform)
+            if (so + need > se) {
                 unsigned long long base = ~0ull;
                 if (lane == 0 && ld_volatile(a.pool_top) + kSlabWords < limit)
                     base = atomicAdd(a.pool_top, (unsigned long long)kSlabWords);
                 base = __shfl_sync(kFull, base, 0);
                 if (base != ~0ull && base + kSlabWords <= a.pool_words) {
-                    wc.slab_off = base;
-                    wc.slab_end = base + kSlabWords;
+                    so = base;
+                    se = base + kSlabWords;
                 }
             }
-            if (wc.slab_off + need <= wc.slab_end) {
-                copy_off = wc.slab_off;
-                wc.slab_off += need;
+            if (so + need <= se) {
+                copy_off = so;
+                so += need;
             }
+            __syncwarp();
+            if (lane == 0) {
+                wc.slab_off = so;
+                wc.slab_end = se;
+            }
+            __syncwarp();
         } else if (words <= kDonateCopyMax) {
             unsigned long long base = ~0ull;
             if (lane == 0 && ld_volatile(a.pool_top) + need < limit) base = atomicAdd(a.pool_top, need);
@@ -1781,7 +1827,7 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
     __syncwarp();
 }
 
-__device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, ResultAcc& acc) {
+__device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, const ResultAcc acc) {
     if (lane_id() == 0) {
         ResultAcc* r = &a.results[graph];
         if (acc.count) atomicAdd(&r->count, acc.count);
@@ -1789,29 +1835,31 @@ __device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, Resu
         if (acc.nodes) atomicAdd(&r->nodes, acc.nodes);
         if (acc.words) atomicAdd(&r->words, acc.words);
     }
-    acc = ResultAcc{};
 }
 
 // Children (lanes in `kids`) of a small-record node (L, Q, P) that no row of
-// Q, nor an earlier row of P, covers: one lane per child, the coverers taken
-// in row order with their rows broadcast by shuffle.  Warp-collective.
-__device__ __forceinline__ uint32_t solve_maximal(uint32_t row, uint32_t L, uint32_t Q, uint32_t P, uint32_t kids) {
+// Q, nor an earlier row of P, covers.  One lane per child x: its coverers are
+// the rows holding every bit of L_x = L & row_x, i.e. the AND over those bits
+// b of col_b (col_b = the rows holding bit b: lane b's `col`, the transpose
+// of the record's rows, fixed for the whole record).  Starting from the rows
+// x may be covered by (Q, and P before x) and ANDing col_b bit by bit, x is
+// maximal iff nothing is left; the loop takes popc(L_x) steps at most and
+// ends as soon as no lane has a candidate coverer left.  Warp-collective.
+__device__ __forceinline__ uint32_t solve_maximal(uint32_t row, uint32_t col, uint32_t L, uint32_t Q, uint32_t P,
+                                                  uint32_t kids) {
     const unsigned lane = lane_id();
-    const uint32_t Lx = L & row;
     const bool mine = (kids >> lane) & 1u;
-    const uint32_t last = 31u - __clz(kids);
-    // P rows at or after the last child cover nothing (Q rows precede all of P)
-    uint32_t J = Q | (P & ((1u << last) - 1u));
-    bool covered = false;
-    for (uint32_t it = 1; J; it++) {
-        const uint32_t j = __ffs(J) - 1;
-        J &= J - 1;
-        const uint32_t rj = __shfl_sync(kFull, row, j);
-        const bool elig = ((Q >> j) & 1u) || j < lane;
-        covered = covered || (mine && elig && (rj & Lx) == Lx);
-        if ((it & 7u) == 0 && !__any_sync(kFull, mine && !covered)) break;
+    uint32_t rem = mine ? (L & row) : 0u;
+    uint32_t cover = mine ? (Q | (P & ((1u << lane) - 1u))) : 0u;
+    while (__any_sync(kFull, rem != 0 && cover != 0)) {
+        const uint32_t b = rem ? __ffs(rem) - 1 : 0u;
+        const uint32_t cb = __shfl_sync(kFull, col, b);
+        if (rem) {
+            cover &= cb;
+            rem &= rem - 1;
+        }
     }
-    return __ballot_sync(kFull, mine && !covered);
+    return __ballot_sync(kFull, mine && cover == 0);
 }
 
 // Enumerates the subtree below the children [next, end) of frame `fdepth`,
@@ -1825,24 +1873,32 @@ __device__ __forceinline__ uint32_t solve_maximal(uint32_t row, uint32_t L, uint
 // frame mirrors level 0 (next = one past the child in progress), so a donor
 // may split the remaining level-0 children off as an ordinary task; the
 // search then drops those it no longer owns.  Warp-collective.
-__device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G, const uint32_t* nd, Frame* frames,
-                                         int fdepth, WarpCtx& wc, ResultAcc& acc, bool donate) {
+__device__ __noinline__ ResultAcc solve_small(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
+                                              Frame* frames, int fdepth, bool donate) {
     const unsigned lane = lane_id();
+    ResultAcc acc{};  // in registers; the caller adds it
     const NodeHdr* h = (const NodeHdr*)nd;
     const RecView R = rec_view(nd);
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t row = lane < n ? R.M[lane] : 0u;
+    // transpose: lane b holds the rows that contain bit b of the record's L
+    uint32_t col = 0;
+#pragma unroll 4
+    for (uint32_t b = 0; b < 32; b++) {
+        const uint32_t cb = __ballot_sync(kFull, (row >> b) & 1u);
+        if (lane == b) col = cb;
+    }
     const unsigned long long eR = lane < n ? G.eR[R.cand[lane]] : 0ull;
     const uint32_t Lroot = R.Lm[0];
     const unsigned long long eL = ((Lroot >> lane) & 1u) ? G.eL[R.map[lane]] : 0ull;  // packed maps hold L vertices
-    SolveLevel* st = wc.solve;
+    SolveLevel* st = s_Solve[warp_in_block()];
     const uint32_t all = n >= 32 ? ~0u : ((1u << n) - 1u);
     const uint32_t Qroot = (1u << nq) - 1u;  // nq < n <= 32
     const uint32_t lo = nq + frames[fdepth].next, hi = nq + frames[fdepth].end;
     const uint32_t kids0 = (hi >= 32 ? ~0u : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
     uint32_t L = Lroot, Q = Qroot, P = all & ~Qroot, nR = h->nRset, Rm = 0;
     unsigned long long sR = h->sR;
-    uint32_t pend = solve_maximal(row, L, Q, P, kids0);
+    uint32_t pend = solve_maximal(row, col, L, Q, P, kids0);
     acc.nodes += __popc(kids0);
     acc.words += n + 32;
     int depth = 0;
@@ -1885,7 +1941,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
             if (a.emit) emit_solved(a, G, nd, Rm | (1u << x) | absorbed, L2);
         }
         if (P2 && l2 >= a.minL && nR2 + __popc(P2) >= a.minR) {
-            const uint32_t pend2 = solve_maximal(row, L2, Q2, P2, P2);
+            const uint32_t pend2 = solve_maximal(row, col, L2, Q2, P2, P2);
             acc.nodes += __popc(P2);
             if (pend2) {
                 if (lane == 0) st[depth] = SolveLevel{L, Q, P, pend, nR, Rm, sR};
@@ -1906,7 +1962,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
             if (donate) {
                 uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
                 if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) {
-                    try_donate(a, frames, fdepth, wc, qh - qt);
+                    try_donate(a, frames, fdepth, qh - qt);
                     const uint32_t hi2 = nq + frames[fdepth].end;  // lowered when level 0 was split
                     const uint32_t keep = hi2 >= 32 ? ~0u : ((1u << hi2) - 1u);
                     if (depth == 0)
@@ -1920,6 +1976,7 @@ __device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G
     }
     if (lane == 0) frames[fdepth].next = frames[fdepth].end;
     __syncwarp();
+    return acc;
 }
 
 #ifdef MBE_PROFILE
@@ -1937,80 +1994,73 @@ __device__ void prof_idle(const EngineArgs& a, unsigned long long t0, unsigned l
 }
 #endif
 
-__global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(EngineArgs a) {
-    __shared__ uint32_t sLi[kWarpsB][kSmemW];
-    __shared__ uint32_t sNz[kWarpsB][kSmemW];
-    __shared__ uint32_t sBucket[kWarpsB][64];
-    __shared__ uint32_t sRow[kWarpsB][kShRows];
-    __shared__ uint32_t sPos[kWarpsB][kShRows];
-    __shared__ unsigned long long sKeys[kWarpsB][kShRows];
-    __shared__ SolveLevel sSolve[kWarpsB][kSolveRows + 1];
+__global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(const __grid_constant__ EngineArgs a) {
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const size_t gw = (size_t)blockIdx.x * kWarpsB + warp;
     Frame* frames = a.frames + gw * a.max_frames;
-    WarpCtx wc;
-    wc.arena = a.arena + gw * a.arena_words;
-    wc.arena_top = 0;
-    // scratch layout (scratch_words): scr_n from the largest root record of
-    // the chunk, kc the power of two >= scr_n
-    uint32_t scr_n = a.scr_n, kc = a.scr_kc;
-    size_t sw = a.scratch_words;
-    if (a.scratch_dyn) {
-        scr_n = max(*(const volatile uint32_t*)a.max_n, 32u);
-        kc = 32;
-        while (kc < scr_n) kc <<= 1;
-        sw = scratch_words(a.max_W, scr_n, kc, a.emit != 0);
+    WarpCtx& wc = s_wc[warp];
+    uint32_t arena_top = 0;  // words of this warp's arena in use (warp-uniform)
+    if (lane == 0) {
+        wc.arena = a.arena + gw * a.arena_words;
+        // scratch layout (scratch_words): scr_n from the largest root record
+        // of the chunk, kc the power of two >= scr_n
+        uint32_t scr_n = a.scr_n, kc = a.scr_kc;
+        size_t sw = a.scratch_words;
+        if (a.scratch_dyn) {
+            scr_n = max(*(const volatile uint32_t*)a.max_n, 32u);
+            kc = 32;
+            while (kc < scr_n) kc <<= 1;
+            sw = scratch_words(a.max_W, scr_n, kc, a.emit != 0);
+        }
+        uint32_t* scr = a.scratch + gw * sw;
+        wc.scrLi = scr;
+        wc.scrNz = scr + a.max_W;
+        wc.scrQcnt = scr + 2 * (size_t)a.max_W;
+        const size_t koff = (2 * (size_t)a.max_W + scr_n + 1) & ~(size_t)1;
+        wc.scrKeysP = (unsigned long long*)(scr + koff);
+        wc.scrKeysQ = wc.scrKeysP + kc;
+        wc.scrPack = (uint32_t*)(wc.scrKeysQ + kc);
+        wc.scrHist = wc.scrPack + 2 * (size_t)kc;
+        wc.scrAbs = wc.scrHist + 32 * (size_t)a.max_W + 32;
+        wc.scr_kc = kc;
+        wc.slab_off = wc.slab_end = 0;
+#ifdef MBE_PROFILE
+        for (int q = 0; q < kProfSlots; q++) wc.prof[q] = 0;
+        wc.last_busy = globaltimer_ns();
+        wc.t_start = wc.last_busy;
+#endif
     }
-    uint32_t* scr = a.scratch + gw * sw;
-    wc.scrLi = scr;
-    wc.scrNz = scr + a.max_W;
-    wc.scrQcnt = scr + 2 * (size_t)a.max_W;
-    size_t koff = (2 * (size_t)a.max_W + scr_n + 1) & ~(size_t)1;
-    wc.scrKeysP = (unsigned long long*)(scr + koff);
-    wc.scrKeysQ = wc.scrKeysP + kc;
-    wc.scrPack = (uint32_t*)(wc.scrKeysQ + kc);
-    wc.scrHist = wc.scrPack + 2 * (size_t)kc;
-    wc.scrAbs = wc.scrHist + 32 * (size_t)a.max_W + 32;
-    wc.scr_kc = kc;
-    wc.sLi = sLi[warp];
-    wc.sNz = sNz[warp];
-    wc.sBucket = sBucket[warp];
-    wc.shRow = sRow[warp];
-    wc.shPos = sPos[warp];
-    wc.shKeys = sKeys[warp];
-    wc.solve = sSolve[warp];
-    wc.slab_off = wc.slab_end = 0;
+    __syncwarp();
 #ifdef MBE_PROFILE
     __shared__ unsigned long long sTab[kProfTB * kProfTC * 2];
     for (int i = threadIdx.x; i < kProfTB * kProfTC * 2; i += blockDim.x) sTab[i] = 0;
     __syncthreads();
-    for (int q = 0; q < kProfSlots; q++) wc.prof[q] = 0;
-    wc.last_busy = globaltimer_ns();
-    wc.t_start = wc.last_busy;
 #endif
     const bool donate = a.variant != MBE_NOWS;
     const bool prefilter = a.variant != MBE_NOES;
     ResultAcc acc{};
     uint32_t evals = 0, evals_reported = 0;
-    Task t{};
-    uint32_t my_path = 0;
     for (;;) {
+        Popped t;
         {
             PROF_T0();
 #ifdef MBE_PROFILE
             unsigned long long w0 = globaltimer_ns();
 #endif
-            bool got = pop_task(a, t, my_path);
+            t = pop_task(a);
             PROF_ADD(wc.prof, kProfPop);
 #ifdef MBE_PROFILE
             if (lane == 0 && a.prof) prof_idle(a, wc.t_start, w0, globaltimer_ns());
 #endif
-            if (!got) break;
+            if (!t.node) break;
         }
         PROF_T0();
+        const uint32_t my_path = t.path;
         const uint32_t graph = ((const NodeHdr*)t.node)->graph;
-        const GraphView G = a.graphs[graph];
-        wc.arena_top = 0;
+        if (lane == 0) s_G[warp] = a.graphs[graph];
+        __syncwarp();
+        const GraphView& G = s_G[warp];
+        arena_top = 0;
         int depth = 0;
         {
             uint32_t p0 = __shfl_sync(kFull, my_path, 0);
@@ -2032,11 +2082,11 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
         for (uint32_t j = 0; j < t.plen; j++) {
             uint32_t idx = __shfl_sync(kFull, my_path, j);
             uint32_t nxt = __shfl_sync(kFull, my_path, (j + 1) & 31);
-            uint32_t mark = wc.arena_top;
+            uint32_t mark = arena_top;
 #ifdef MBE_PROFILE
             long long c0r = clock64();
 #endif
-            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, wc, acc, true, false);
+            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, arena_top, acc, true, false);
 #ifdef MBE_PROFILE
             PROF_TAB(8, c0r, clock64() - c0r);
 #endif
@@ -2045,7 +2095,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                 replay_ok = false;
                 break;
             }
-            wc.arena_top += co.size;
+            arena_top += co.size;
             depth = (int)j + 1;
             if (lane == 0) {
                 Frame nf;
@@ -2078,7 +2128,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                 __syncwarp();
             } else {
                 if (f.next >= f.end) {
-                    wc.arena_top = f.arena_mark;
+                    arena_top = f.arena_mark;
                     depth--;
                     continue;
                 }
@@ -2087,7 +2137,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                     uint32_t qh = ld_volatile(a.q_head), qt = ld_volatile(a.q_tail), qd = ld_volatile(a.q_done);
                     if ((int)(qh - qt) > 0 && (qt - qd) + a.q_margin < a.task_cap) {
                         PROF_T0();
-                        try_donate(a, frames, depth, wc, qh - qt);
+                        try_donate(a, frames, depth, qh - qt);
                         PROF_ADD(wc.prof, kProfDonate);
                     }
                     f = frames[depth];
@@ -2096,7 +2146,11 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                 const uint32_t* nd = (const uint32_t*)f.node;
                 if (prefilter && (((const NodeHdr*)nd)->flags & kRecPacked) && ((const NodeHdr*)nd)->n <= a.solve_rows) {
                     PROF_T0();
-                    solve_small(a, G, nd, frames, depth, wc, acc, donate);
+                    const ResultAcc sa = solve_small(a, G, nd, frames, depth, donate);
+                    acc.count += sa.count;
+                    acc.hash += sa.hash;
+                    acc.nodes += sa.nodes;
+                    acc.words += sa.words;
                     PROF_ADD(wc.prof, kProfSolve);
                     continue;
                 }
@@ -2133,12 +2187,12 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                 }
                 __syncwarp();
             }
-            uint32_t mark = wc.arena_top;
+            uint32_t mark = arena_top;
 #ifdef MBE_PROFILE
             long long c0e = clock64();
             const uint32_t pW = ((const NodeHdr*)f.node)->W;
 #endif
-            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, wc, acc, false, known_max);
+            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, arena_top, acc, false, known_max);
 #ifdef MBE_PROFILE
             PROF_TAB(min(7, 31 - __clz(pW)), c0e, clock64() - c0e);
             if ((((const NodeHdr*)f.node)->flags & kRecPacked) && ((const NodeHdr*)f.node)->n <= 32)
@@ -2157,7 +2211,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
                     if (lane == 0) set_error(a, kErrFrames, depth);
                     break;
                 }
-                wc.arena_top += co.size;
+                arena_top += co.size;
                 depth++;
                 if (lane == 0) {
                     Frame nf;
@@ -2175,6 +2229,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(Engi
             if ((evals & 7u) == 0 && ld_volatile(a.error)) break;
         }
         flush_acc(a, graph, acc);
+        acc = ResultAcc{};
         if (lane == 0) {
             __threadfence();
             atomicSub(a.pending, 1);

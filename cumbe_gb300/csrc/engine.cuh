@@ -26,14 +26,16 @@
 namespace mbe {
 
 // Shape of the DFS kernel: warps per block and the resident blocks per SM
-// it is compiled for (the register budget).  4 x 5 = 20 warps per SM at 96
-// registers measured fastest (8 x 2 at 128 registers: +3%; 8 x 3 at 80 with
-// spills: +6%).
+// it is compiled for (the register budget).  4 x 6 = 24 warps per SM at 80
+// registers measured fastest once the warp-uniform state moved from local
+// to shared memory (bench graph: 5 blocks 254.5 ms, 6 blocks 248.0 ms,
+// 8 blocks 264 ms; with 6 blocks the shared arrays are trimmed so the six
+// fit a 64 KB carveout: 246.3 ms).
 #ifndef MBE_DFS_WARPS
 #define MBE_DFS_WARPS 4
 #endif
 #ifndef MBE_DFS_MIN_BLOCKS
-#define MBE_DFS_MIN_BLOCKS 5
+#define MBE_DFS_MIN_BLOCKS 6
 #endif
 constexpr int kDfsWarps = MBE_DFS_WARPS;
 
