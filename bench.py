@@ -186,59 +186,94 @@ def cpu_baseline(csr, wl, threads, stride_mult=1):
 
 
 def batched_leg(eng, n_graphs=4096):
-    """Batched workload: n_graphs graphs (workloads.batch) in one launch pair
-    vs one launch pair per graph; per-graph counts and hashes must agree."""
+    """Batched workload: n_graphs graphs (workloads.batch) through
+    mbe_batch_run with the engine defaults, then autotuned (mbe_batch_tune
+    on the same graphs, its wall time reported apart), vs one launch pair per
+    graph.  Per-graph counts and hashes must agree between all three and
+    with the committed oracle results for the graphs they cover."""
     import cumbe_gb300 as cm
     from cumbe_gb300 import workloads
     ps = workloads.batch(n_graphs)
     gs = [cm.Graph.generate(**p) for p in ps]
     for g in gs:
         eng.upload(g)
+    eng.batch_tune_reset()
     eng.batch(gs[:64])  # warm-up
     t0 = time.perf_counter()
     res, ms = eng.batch(gs)
     batched_wall = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    choices = eng.batch_tune(gs)
+    tune_wall = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    res_t, ms_t = eng.batch(gs)
+    tuned_wall = (time.perf_counter() - t0) * 1e3
+    eng.batch_tune_reset()
     plain_ms = 0.0
     mismatches = 0
     t0 = time.perf_counter()
-    for g, r in zip(gs, res):
+    for g, r, rt in zip(gs, res, res_t):
         q = eng.enumerate(g)
         plain_ms += q.ms
-        mismatches += (q.count, q.hash) != (r.count, r.hash)
+        mismatches += (q.count, q.hash) != (r.count, r.hash) or (rt.count, rt.hash) != (r.count, r.hash)
     plain_wall = (time.perf_counter() - t0) * 1e3
+    fix = json.load(open(os.path.join(ROOT, "tests", "golden", "batch_oracle.json")))["graphs"]
+    fixture_checked = fixture_mismatches = 0
+    for seed, r in enumerate(res_t):
+        if str(seed) in fix:
+            fixture_checked += 1
+            fixture_mismatches += [r.count, f"{r.hash:#018x}"] != fix[str(seed)]
     total = sum(r.count for r in res)
     for g in gs:
         eng.release(g)
-    return {"graphs": n_graphs, "bicliques": total, "batched_ms": ms, "plain_ms": plain_ms,
-            "batched_wall_ms": batched_wall, "plain_wall_ms": plain_wall,
-            "batched_bicliques_per_s": total / (ms / 1e3), "plain_bicliques_per_s": total / (plain_ms / 1e3),
+    return {"graphs": n_graphs, "bicliques": total, "batched_ms": ms, "tuned_ms": ms_t, "plain_ms": plain_ms,
+            "batched_wall_ms": batched_wall, "tuned_wall_ms": tuned_wall, "plain_wall_ms": plain_wall,
+            "tuning_wall_ms": tune_wall,
+            "batched_bicliques_per_s": total / (ms / 1e3), "tuned_bicliques_per_s": total / (ms_t / 1e3),
+            "plain_bicliques_per_s": total / (plain_ms / 1e3),
+            "tune_choices": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in c.items()} for c in choices],
             "note": "_ms = device time of the enumeration kernels (CUDA events); _wall_ms = host wall clock "
-                    "of the whole call(s), graphs resident",
+                    "of the whole call(s), graphs resident; tuning = mbe_batch_tune's sweep, untimed",
             "per_graph_mismatches": mismatches,
+            "oracle_fixture": {"graphs_checked": fixture_checked, "mismatches": fixture_mismatches},
             "workload": "4,096 uniform random graphs, |U| log-uniform [50,5000], |V|=|U|/2, "
                         "density log-uniform [0.002,0.05], seeds 0..4095"}
 
 
-def served_leg(rate=2000.0, n_requests=4000, seed=11):
-    """Poisson request stream against a device-resident pool: continuous
-    batching (2 slots of 2 DFS blocks per SM each, up to 256 requests per launch)
-    vs one request per launch on the whole GPU.  Half the requests are
-    thresholded (|A| >= a, |B| >= b, a, b uniform in 1..5)."""
+_SERVED_POOL = None
+
+
+def served_leg(rate=2000.0, n_requests=8000, seed=11):
+    """Poisson request stream against a device-resident pool drawn from the
+    four other workloads (workloads.served_pool: the 2,000 x 1,000 graph, the
+    94,000 x 30,000 graph, the stress shape at 1/250 and 1/100, the batch
+    graphs with |U| <= 1000), each request on a uniformly drawn pool graph,
+    half of them thresholded (|A| >= a, |B| >= b, a, b uniform in 1..5).
+    Continuous batching (2 slots of 3 DFS blocks per SM, up to 256 requests
+    per launch) vs one request per launch on the whole GPU; both arms are
+    warmed up (buffers sized for the pool) before the stream starts."""
+    global _SERVED_POOL
     import numpy as np
     import cumbe_gb300 as cm
     from cumbe_gb300 import workloads
-    pool = [cm.Graph.generate(**workloads.SINGLE["power_law_2k_1k"])]
-    pool += [cm.Graph.generate(**p) for p in workloads.batch(4096) if p["n_rows"] <= 1000]
+    if _SERVED_POOL is None:
+        spec = workloads.served_pool()
+        _SERVED_POOL = ([name for name, _ in spec], [cm.Graph.generate(**p) for _, p in spec])
+    names, pool = _SERVED_POOL
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, n_requests)
     picks = rng.integers(0, len(pool), n_requests)
     thr = [(0, 0) if rng.random() < 0.5 else (int(rng.integers(1, 6)), int(rng.integers(1, 6)))
            for _ in range(n_requests)]
+    mix = {}
+    for k in picks:
+        mix[names[k]] = mix.get(names[k], 0) + 1
 
     def run(slots, max_batch, bpsm):
         srv = cm.Server(0, slots=slots, max_batch=max_batch, blocks_per_sm=bpsm)
         try:
             gids = [srv.add_graph(g) for g in pool]
+            srv.warmup()
             t0 = time.perf_counter()
             due = 0.0
             for i in range(n_requests):
@@ -251,6 +286,7 @@ def served_leg(rate=2000.0, n_requests=4000, seed=11):
             while len(out) < n_requests:
                 out += srv.poll()
                 time.sleep(0.001)
+            mem = srv.memory()
         finally:
             srv.stop()
         lat = np.array([r["done_s"] - r["submit_s"] for r in out]) * 1e3
@@ -259,16 +295,18 @@ def served_leg(rate=2000.0, n_requests=4000, seed=11):
         ok = all(r["status"] == 0 for r in out)
         res = {(r["request"]): (r["count"], r["hash"]) for r in out}
         return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "requests_per_s": n_requests / span, "bicliques_per_s": tot / span, "all_ok": ok,
-                "mean_batch": float(np.mean([r["batch_size"] for r in out]))}, res
+                "max_ms": float(lat.max()), "requests_per_s": n_requests / span, "bicliques_per_s": tot / span,
+                "all_ok": ok, "mean_batch": float(np.mean([r["batch_size"] for r in out])),
+                "search_bytes": mem["search_bytes"], "graph_bytes": mem["graph_bytes"]}, res
 
-    cont, r1 = run(2, 256, 2)
+    cont, r1 = run(2, 256, 3)
     plain, r2 = run(1, 1, 0)
     same = [r1[k] for k in sorted(r1)] == [r2[k] for k in sorted(r2)]
-    return {"rate_req_per_s": rate, "requests": n_requests, "pool_graphs": len(pool),
+    return {"rate_req_per_s": rate, "requests": n_requests, "pool_graphs": len(pool), "request_mix": mix,
             "continuous_batching": cont, "one_request_per_launch": plain,
-            "results_identical": same,
-            "pool": "the 2,000 x 1,000 power-law graph + the batch graphs with |U| <= 1000"}
+            "results_identical": same, "mem_budget_bytes": 120 << 30,
+            "pool": "workloads.served_pool(): the 2,000 x 1,000 and 94,000 x 30,000 graphs, the stress shape at "
+                    "1/250 and 1/100, and the batch graphs with |U| <= 1000"}
 
 
 def stress_leg(eng):

@@ -68,6 +68,13 @@ class _Result(ctypes.Structure):
                 ("ms", ctypes.c_float), ("ms_prep", ctypes.c_float)]
 
 
+class _TuneChoice(ctypes.Structure):
+    _fields_ = [("bucket", ctypes.c_uint32), ("n_graphs", ctypes.c_uint32), ("sample_graphs", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32), ("donate_min", ctypes.c_uint32), ("solve_rows", ctypes.c_uint32),
+                ("chunk_mwords", ctypes.c_uint32), ("trials", ctypes.c_uint32), ("ms_default", ctypes.c_float),
+                ("ms_tuned", ctypes.c_float)]
+
+
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
                 ("variant", ctypes.c_uint32), ("mem_budget", ctypes.c_uint64)]
@@ -104,6 +111,9 @@ SIGNATURES = {
     "mbe_enumerate": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.POINTER(_Opts), ctypes.POINTER(_Result)]),
     "mbe_batch_run": (ctypes.c_int, [_VP, ctypes.POINTER(_VP), ctypes.c_uint32, ctypes.c_int,
                                      ctypes.POINTER(_Opts), ctypes.POINTER(_Result), ctypes.POINTER(ctypes.c_float)]),
+    "mbe_batch_tune": (ctypes.c_int, [_VP, ctypes.POINTER(_VP), ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(_Opts),
+                                      ctypes.POINTER(_TuneChoice), ctypes.c_uint32, _U32P]),
+    "mbe_batch_tune_reset": (ctypes.c_int, [_VP]),
     "mbe_biclique_hash": (ctypes.c_uint64, [_U32P, ctypes.c_uint32, _U32P, ctypes.c_uint32]),
     "mbe_variant_name": (ctypes.c_char_p, [ctypes.c_int]),
     "mbe_variant_from_name": (ctypes.c_int, [ctypes.c_char_p]),
@@ -115,6 +125,8 @@ SIGNATURES = {
     "mbe_server_submit": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _U64P]),
     "mbe_server_poll": (ctypes.c_int, [_VP, ctypes.POINTER(_RequestResult), ctypes.c_uint32, _U32P]),
     "mbe_server_clock": (ctypes.c_double, [_VP]),
+    "mbe_server_warmup": (ctypes.c_int, [_VP]),
+    "mbe_server_memory": (ctypes.c_int, [_VP, _U64P, _U64P, _U64P]),
     "mbe_server_stop": (ctypes.c_int, [_VP]),
     "mbe_enumerate_static": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, _VP, _VP, _VP, _VP, ctypes.c_int,
                                             _VP, _VP]),
@@ -340,6 +352,23 @@ class Engine:
                "mbe_batch_run")
         return [Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep) for r in res], tot.value
 
+    def batch_tune(self, graphs: list[Graph], variant: str = "cuMBE", min_rows: int = 0,
+                   min_cols: int = 0) -> list[dict]:
+        """Autotunes the batched mode for the size buckets of `graphs`
+        (mbe_batch_tune); later batch() calls on this device use the
+        choices.  Returns one dict per bucket."""
+        n = len(graphs)
+        arr = (_VP * n)(*[g.handle for g in graphs])
+        out = (_TuneChoice * 16)()
+        k = ctypes.c_uint32()
+        o = _opts(min_rows=min_rows, min_cols=min_cols)
+        _check(lib().mbe_batch_tune(self._h, arr, n, VARIANTS[variant], ctypes.byref(o), out, 16, ctypes.byref(k)),
+               "mbe_batch_tune")
+        return [{f: getattr(out[i], f) for f, _ in _TuneChoice._fields_} for i in range(k.value)]
+
+    def batch_tune_reset(self):
+        _check(lib().mbe_batch_tune_reset(self._h), "mbe_batch_tune_reset")
+
     def counters(self) -> dict:
         """Cumulative kernel launches and host<->device bytes of this context."""
         l, h, d = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
@@ -367,7 +396,7 @@ class Server:
     (mbe_server_*).  Requests are answered asynchronously; poll() returns
     finished ones with their timestamps on the server clock."""
 
-    def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 2,
+    def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 3,
                  variant: str = "cuMBE", mem_budget: int = 0):
         cfg = _ServerConfig(slots, max_batch, blocks_per_sm, VARIANTS[variant], mem_budget)
         self._h = _VP()
@@ -396,6 +425,19 @@ class Server:
 
     def clock(self) -> float:
         return lib().mbe_server_clock(self._h)
+
+    def warmup(self):
+        """Sizes every slot's buffers for the graphs added so far (blocks
+        until done)."""
+        _check(lib().mbe_server_warmup(self._h), "mbe_server_warmup")
+
+    def memory(self) -> dict:
+        """Device bytes held: the slots' search buffers, the resident graphs,
+        and the cap of one slot."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().mbe_server_memory(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "mbe_server_memory")
+        return {"search_bytes": a.value, "graph_bytes": b.value, "slot_cap": c.value}
 
     def stop(self):
         if self._h and self._h.value:

@@ -1,7 +1,9 @@
 // C ABI of libmbe: contexts, device residency, enumeration, batching.
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <new>
 #include <unordered_map>
 #include <vector>
@@ -146,7 +148,7 @@ namespace mbe {
 // once per orientation group.
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
                     mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
-                    const EmitTarget* emit) {
+                    const EmitTarget* emit, uint64_t mem_cap, const BatchKnobs* knobs) {
     const uint32_t n = (uint32_t)devs.size();
     bool any_swapped = false, any_plain = false;
     for (const DeviceGraph* d : devs) (d->swapped ? any_swapped : any_plain) = true;
@@ -180,11 +182,18 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
                 if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
         EngineConfig cfg = make_config(variant, opts, sw);
         cfg.emit = emit;
+        cfg.mem_cap = mem_cap;
         // Many graphs: chunks of ~128 MiB of root records, so that the DFS
         // reads each chunk's records while they are still in L2 (measured:
         // 4,096 mixed graphs 19.4 s -> 17.2 s).  One graph keeps one chunk:
         // every chunk ends in a load-imbalance tail, which costs more there.
         if (n > 1 && !cfg.pool_words) cfg.chunk_words = 32ull << 20;
+        if (knobs) {
+            if (knobs->blocks_per_sm) cfg.blocks_per_sm = knobs->blocks_per_sm;
+            if (knobs->donate_min) cfg.donate_min = knobs->donate_min;
+            cfg.solve_rows = knobs->solve_rows;
+            if (knobs->chunk_words && !cfg.pool_words) cfg.chunk_words = knobs->chunk_words;
+        }
         std::vector<ResultAcc> part;
         EngineStats ps;
         mbe_status st = engine_run(eb, s, cfg, devs, split ? sel : roots, part, &ps, io);
@@ -269,6 +278,167 @@ struct EmitRun {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Batched mode: autotuning of the engine knobs per graph-size bucket.
+//
+// A graph's bucket is its branching side's size class (|R| < 256, < 1024,
+// < 4096, larger) and its average degree class (E/|R| < 4, < 16, < 64,
+// larger).  mbe_batch_tune times, for each bucket present in a batch, a
+// sample of the bucket's graphs (up to 32, spread over the bucket's range of
+// edge counts) under a coordinate descent over four knobs -- DFS blocks per
+// SM (block count), donation granularity (steal granularity), the register
+// search's row limit (bitmap search in registers vs records in memory) and
+// the root-record chunk (how much search state is live at once) -- keeping
+// a change only when it is 3% faster, and caches the choice per (device,
+// variant, bucket) for the process.  mbe_batch_run applies cached choices.
+namespace {
+
+constexpr uint32_t kTuneSample = 32;
+
+uint32_t tune_bucket(const DeviceGraph& d) {
+    const uint32_t nR = d.nR - d.n_isolated;
+    const double deg = nR ? (double)d.nE / nR : 0.0;
+    const uint32_t rc = nR < 256 ? 0 : nR < 1024 ? 1 : nR < 4096 ? 2 : 3;
+    const uint32_t dc = deg < 4 ? 0 : deg < 16 ? 1 : deg < 64 ? 2 : 3;
+    return 4 * rc + dc;
+}
+
+struct TuneKey {
+    int device;
+    uint32_t variant, bucket;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(device, variant, bucket) < std::tie(o.device, o.variant, o.bucket);
+    }
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, mbe_tune_choice> g_tune;
+
+bool explicit_tuning(const mbe_opts* o) { return o && (o->blocks_per_sm || o->donate_min || o->stack_words); }
+
+BatchKnobs knobs_of(const mbe_tune_choice& c) {
+    BatchKnobs k;
+    k.blocks_per_sm = c.blocks_per_sm;
+    k.donate_min = c.donate_min;
+    k.solve_rows = c.solve_rows;
+    k.chunk_words = (uint64_t)c.chunk_mwords << 20;
+    return k;
+}
+
+}  // namespace
+
+extern "C" mbe_status mbe_batch_tune(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
+                                     const mbe_opts* opts, mbe_tune_choice* out, uint32_t cap, uint32_t* n_out) {
+    clear_error();
+    if (!ctx || (!graphs && n) || (!out && cap)) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    if (explicit_tuning(opts)) return fail(MBE_ERR_INVALID_ARG, "mbe_batch_tune chooses the tuning fields itself");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    mbe_status st = check_opts(opts);
+    if (st) return st;
+    if ((st = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"))) return st;
+    std::map<uint32_t, std::vector<const DeviceGraph*>> buckets;
+    for (uint32_t i = 0; i < n; i++) {
+        if (!graphs[i]) return fail(MBE_ERR_INVALID_ARG, "null graph");
+        const DeviceGraph* d;
+        if ((st = ensure_resident(ctx, graphs[i], &d))) return st;
+        buckets[tune_bucket(*d)].push_back(d);
+    }
+    int occB = 0;
+    if ((st = check_cuda(dfs_blocks_per_sm(ctx->device, &occB), "occupancy"))) return st;
+    uint32_t k_out = 0;
+    for (auto& kv : buckets) {
+        std::vector<const DeviceGraph*>& all = kv.second;
+        std::stable_sort(all.begin(), all.end(), [](const DeviceGraph* a, const DeviceGraph* b) { return a->nE > b->nE; });
+        std::vector<const DeviceGraph*> sample;
+        const size_t m = std::min<size_t>(all.size(), kTuneSample);
+        for (size_t j = 0; j < m; j++) sample.push_back(all[j * all.size() / m]);
+        uint32_t trials = 0;
+        uint64_t ref_count = 0;
+        bool have_ref = false;
+        auto measure = [&](const BatchKnobs& k, float* ms) -> mbe_status {
+            float best = 0;
+            for (int rep = 0; rep < 2; rep++) {
+                std::vector<ResultAcc> acc;
+                EngineStats stats;
+                mbe_status s2 = run_devs(ctx->eb, ctx->stream, &ctx->io, sample, variant, opts, acc, stats, nullptr, 0, &k);
+                if (s2) return s2;
+                uint64_t c = 0;
+                for (const ResultAcc& r : acc) c += r.count;
+                if (have_ref && c != ref_count) return fail(MBE_ERR_CUDA, "autotuner: results differ between configurations");
+                ref_count = c;
+                have_ref = true;
+                const float t = stats.ms_expand + stats.ms_dfs;
+                if (rep == 0 || t < best) best = t;
+                if (t > 200.0f) break;  // heavy samples: one timing is enough
+            }
+            trials++;
+            *ms = best;
+            return MBE_OK;
+        };
+        BatchKnobs cur;  // engine defaults
+        cur.chunk_words = 32ull << 20;
+        float best = 0, ms_default = 0;
+        if ((st = measure(cur, &best))) return st;
+        // heavy buckets: thin the sample (every other graph) until a run
+        // takes under ~400 ms, so that the sweep stays short
+        while (best > 400.0f && sample.size() > 2) {
+            std::vector<const DeviceGraph*> thin;
+            for (size_t j = 0; j < sample.size(); j += 2) thin.push_back(sample[j]);
+            sample.swap(thin);
+            have_ref = false;
+            if ((st = measure(cur, &best))) return st;
+        }
+        ms_default = best;
+        const uint32_t b_alt[2] = {(uint32_t)std::max(1, occB - 2), (uint32_t)std::max(1, occB / 2)};
+        const uint32_t d_alt[2] = {3, 4};
+        const uint32_t s_alt[2] = {16, 0};
+        const uint64_t c_alt[2] = {8ull << 20, 128ull << 20};
+        for (int knob = 0; knob < 4; knob++)
+            for (int j = 0; j < 2; j++) {
+                BatchKnobs k2 = cur;
+                if (knob == 0) k2.blocks_per_sm = b_alt[j];
+                if (knob == 1) k2.donate_min = d_alt[j];
+                if (knob == 2) k2.solve_rows = s_alt[j];
+                if (knob == 3) k2.chunk_words = c_alt[j];
+                float t = 0;
+                if ((st = measure(k2, &t))) return st;
+                if (t < 0.97f * best) {
+                    best = t;
+                    cur = k2;
+                }
+            }
+        mbe_tune_choice c;
+        std::memset(&c, 0, sizeof c);
+        c.bucket = kv.first;
+        c.n_graphs = (uint32_t)all.size();
+        c.sample_graphs = (uint32_t)sample.size();
+        c.blocks_per_sm = cur.blocks_per_sm;
+        c.donate_min = cur.donate_min;
+        c.solve_rows = cur.solve_rows;
+        c.chunk_mwords = (uint32_t)(cur.chunk_words >> 20);
+        c.trials = trials;
+        c.ms_default = ms_default;
+        c.ms_tuned = best;
+        {
+            std::lock_guard<std::mutex> tl(g_tune_mu);
+            g_tune[TuneKey{ctx->device, (uint32_t)variant, kv.first}] = c;
+        }
+        if (k_out < cap) out[k_out] = c;
+        k_out++;
+    }
+    if (n_out) *n_out = std::min(k_out, cap);
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_batch_tune_reset(mbe_ctx* ctx) {
+    clear_error();
+    if (!ctx) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> tl(g_tune_mu);
+    for (auto it = g_tune.begin(); it != g_tune.end();)
+        it = it->first.device == ctx->device ? g_tune.erase(it) : std::next(it);
+    return MBE_OK;
+}
+
 static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
                              const mbe_opts* opts, mbe_result* out, float* total_ms) {
     const bool emit = opts && (opts->flags & MBE_OPT_EMIT);
@@ -286,8 +456,44 @@ static mbe_status run_graphs(mbe_ctx* ctx, const mbe_graph* const* graphs, uint3
     if (emit && (st = er.setup(ctx, opts))) return st;
     std::vector<ResultAcc> acc;
     EngineStats stats;
-    if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, devs, variant, opts, acc, stats, emit ? &er.t : nullptr)))
+    // graphs whose bucket mbe_batch_tune has tuned on this device run with
+    // the cached choice, one launch pair per distinct choice
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, std::vector<uint32_t>> groups;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, BatchKnobs> group_knobs;
+    if (n > 1 && !explicit_tuning(opts)) {
+        std::lock_guard<std::mutex> tl(g_tune_mu);
+        if (!g_tune.empty())
+            for (uint32_t i = 0; i < n; i++) {
+                auto it = g_tune.find(TuneKey{ctx->device, (uint32_t)variant, tune_bucket(*devs[i])});
+                BatchKnobs k;
+                k.chunk_words = 32ull << 20;
+                if (it != g_tune.end()) k = knobs_of(it->second);
+                const auto key = std::make_tuple(k.blocks_per_sm, k.donate_min, k.solve_rows, (uint32_t)(k.chunk_words >> 20));
+                groups[key].push_back(i);
+                group_knobs[key] = k;
+            }
+    }
+    if (!groups.empty()) {
+        acc.assign(n, ResultAcc{});
+        for (auto& kv : groups) {
+            std::vector<const DeviceGraph*> sub;
+            for (uint32_t i : kv.second) sub.push_back(devs[i]);
+            std::vector<ResultAcc> part;
+            EngineStats ps;
+            if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, sub, variant, opts, part, ps, nullptr, 0,
+                               &group_knobs[kv.first])))
+                return st;
+            for (size_t j = 0; j < kv.second.size(); j++) acc[kv.second[j]] = part[j];
+            stats.ms_expand += ps.ms_expand;
+            stats.ms_dfs += ps.ms_dfs;
+            stats.chunks += ps.chunks;
+            stats.grid_a = ps.grid_a;
+            stats.grid_b = ps.grid_b;
+        }
+    } else if ((st = run_devs(ctx->eb, ctx->stream, &ctx->io, devs, variant, opts, acc, stats,
+                              emit ? &er.t : nullptr))) {
         return st;
+    }
     ctx->last_stats = stats;
     for (uint32_t i = 0; i < n; i++) {
         mbe_result& r = out[i];

@@ -2251,17 +2251,29 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
 #endif
 }
 
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // host driver
 
+size_t EngineBuffers::bytes() const {
+    size_t t = 0;
+    for (const DevBuf* b : {&graphs, &roots, &ctrl, &tasks, &ready, &cmap, &a_cl, &a_cnt, &a_keys, &pool, &arena, &frames,
+                            &scratch, &results, &retry_in, &retry_list, &e_ids, &e_start, &e_nrows, &e_ncols, &e_ctl})
+        t += b->bytes;
+    return t;
+}
+
 void EngineBuffers::release() {
     for (DevBuf* b : {&graphs, &roots, &ctrl, &tasks, &ready, &cmap, &a_cl, &a_cnt, &a_keys, &pool, &arena, &frames,
                       &scratch, &results, &retry_in, &retry_list, &e_ids, &e_start, &e_nrows, &e_ncols, &e_ctl})
         b->free();
+    for (cudaEvent_t& e : ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    cmap_clean = ready_clean = 0;
 }
 
 mbe_status DevBuf::ensure(size_t need) {
@@ -2349,6 +2361,42 @@ static cudaError_t try_dfs_carveout() {
     return cudaSuccess;
 }
 
+// SM count and the two kernels' resident blocks per SM (after the DFS
+// carveout is applied), looked up once per device: they do not change, and
+// the queries cost host time on every small request otherwise.
+static cudaError_t device_facts(int dev, int* n_sm, int* occA, int* occB) {
+    constexpr int kMaxDev = 128;
+    static std::mutex mu;
+    static int facts[kMaxDev][3];
+    static bool known[kMaxDev] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 0 || dev >= kMaxDev || !known[dev]) {
+        int f[3] = {0, 0, 0};
+        cudaError_t e = cudaDeviceGetAttribute(&f[0], cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[1], expand_roots_kernel, kThreadsA, 0);
+        if (e == cudaSuccess) e = try_dfs_carveout();
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[2], dfs_kernel, kThreadsB, 0);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < kMaxDev) {
+            std::memcpy(facts[dev], f, sizeof f);
+            known[dev] = true;
+        }
+        *n_sm = f[0];
+        *occA = f[1];
+        *occB = f[2];
+        return cudaSuccess;
+    }
+    *n_sm = facts[dev][0];
+    *occA = facts[dev][1];
+    *occB = facts[dev][2];
+    return cudaSuccess;
+}
+
+cudaError_t dfs_blocks_per_sm(int dev, int* occ) {
+    int n_sm = 0, occA = 0;
+    return device_facts(dev, &n_sm, &occA, occ);
+}
+
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
                       const std::vector<const DeviceGraph*>& gs, const std::vector<uint2>& roots,
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io) {
@@ -2373,12 +2421,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     }());
     int dev = 0;
     MBE_CUDA_TRY(cudaGetDevice(&dev));
-    int n_sm = 0;
-    MBE_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-    int occA = 0, occB = 0;
-    MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, expand_roots_kernel, kThreadsA, 0));
-    MBE_CUDA_TRY(try_dfs_carveout());
-    MBE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occB, dfs_kernel, kThreadsB, 0));
+    int n_sm = 0, occA = 0, occB = 0;
+    MBE_CUDA_TRY(device_facts(dev, &n_sm, &occA, &occB));
     // root expansion at full occupancy (4 blocks per SM measured 23 -> 15 ms
     // on the 94k x 30k graph against 2), or within the share of the GPU a
     // caller asked for (server slots that run side by side)
@@ -2394,9 +2438,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     // Per-warp DFS arenas default to 4 MiB each (at most 30% of free device
     // memory in total); the shared node pool starts at 8 GiB and is doubled
     // (up to 60% of free memory) whenever a run exhausts it.
-    size_t free_b = 0, tot_b = 0;
-    MBE_CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
     if (!eb.arena_words) {
+        size_t free_b = 0, tot_b = 0;
+        MBE_CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
         uint64_t cap = (uint64_t)(free_b * 0.30) / nwarpsB / 4;
         uint64_t want = 1u << 20;
         if (const char* env = std::getenv("MBE_ARENA_WORDS")) want = std::strtoull(env, nullptr, 10);
@@ -2409,8 +2453,39 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             if (mb) eb.pool_words = mb * (1ull << 20) / 4;
         }
     }
-    const uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
+    uint32_t arena_words = cfg.arena_words ? std::min(cfg.arena_words, eb.arena_words) : eb.arena_words;
     const uint32_t retry_cap = 1u << 16;
+    // Under a memory cap the arenas take at most a quarter of it, and the
+    // node pool what the other buffers (as they will be held after this
+    // call: DevBuf only grows) leave.
+    uint64_t pool_cap_words = ~0ull;
+    if (cfg.mem_cap) {
+        arena_words = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(arena_words, cfg.mem_cap / 4 / nwarpsB / 4),
+                                                   1u << 12) & ~31u;
+        const uint32_t scr_b = std::max<uint32_t>(maxNR, 32);
+        size_t kc_b = 32;
+        while (kc_b < scr_b) kc_b <<= 1;
+        auto held = [](const DevBuf& b, size_t need) { return std::max(b.bytes, std::max(need, (size_t)256)); };
+        const size_t fixed =
+            held(eb.graphs, sizeof(GraphView) * ng) + held(eb.roots, sizeof(uint2) * roots.size()) +
+            held(eb.ctrl, sizeof(Ctrl)) + held(eb.tasks, sizeof(Task) * (size_t)task_cap) +
+            held(eb.ready, sizeof(uint32_t) * (size_t)task_cap) + held(eb.cmap, sizeof(int) * (size_t)gridA * maxNR) +
+            held(eb.a_cl, sizeof(uint32_t) * (size_t)gridA * maxNR) +
+            held(eb.a_cnt, sizeof(uint32_t) * (size_t)gridA * maxNR) +
+            held(eb.a_keys, sizeof(unsigned long long) * (size_t)gridA * keys_cap) +
+            held(eb.arena, sizeof(uint32_t) * (size_t)nwarpsB * arena_words) +
+            held(eb.frames, sizeof(Frame) * (size_t)nwarpsB * max_frames) + held(eb.results, sizeof(ResultAcc) * ng) +
+            held(eb.retry_in, sizeof(uint32_t) * (size_t)retry_cap) +
+            held(eb.retry_list, sizeof(uint2) * roots.size()) +
+            held(eb.scratch, sizeof(uint32_t) * (size_t)nwarpsB * scratch_words(maxW, scr_b, kc_b, cfg.emit != nullptr));
+        const size_t min_pool = 16u << 20;
+        if (fixed + min_pool > cfg.mem_cap)
+            return fail(MBE_ERR_OUT_OF_MEMORY, "memory cap of " + std::to_string(cfg.mem_cap) + " bytes is below the " +
+                                                   std::to_string(fixed + min_pool) + " bytes this run needs");
+        pool_cap_words = ((cfg.mem_cap - fixed) / 4) & ~31ull;
+        eb.pool_words = std::min<uint64_t>(eb.pool_words, pool_cap_words);
+        if (eb.pool.bytes > sizeof(uint32_t) * pool_cap_words) eb.pool.free();  // reallocated below, smaller
+    }
 
     mbe_status st;
     std::vector<GraphView> views;
@@ -2425,7 +2500,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     if ((st = eb.a_cl.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
     if ((st = eb.a_cnt.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
     if ((st = eb.a_keys.ensure(sizeof(unsigned long long) * (size_t)gridA * keys_cap))) return st;
-    if ((st = eb.arena.ensure(sizeof(uint32_t) * (size_t)nwarpsB * eb.arena_words))) return st;
+    if ((st = eb.arena.ensure(sizeof(uint32_t) * (size_t)nwarpsB * arena_words))) return st;
     if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * max_frames))) return st;
     if ((st = eb.results.ensure(sizeof(ResultAcc) * ng))) return st;
     if ((st = eb.retry_in.ensure(sizeof(uint32_t) * (size_t)retry_cap))) return st;
@@ -2443,7 +2518,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.minR = cfg.minR;
     a.donate_min = std::max(2u, cfg.donate_min);
     a.donate_copy = 1;
-    a.solve_rows = kSolveRows;
+    a.solve_rows = std::min<uint32_t>(cfg.solve_rows, kSolveRows);
     if (const char* e = std::getenv("MBE_SOLVE_ROWS")) a.solve_rows = std::min<uint32_t>((uint32_t)std::atoi(e), kSolveRows);
     if (const char* e = std::getenv("MBE_DONATE_COPY")) a.donate_copy = (uint32_t)std::atoi(e);
     a.root_next = &ctrl->root_next;
@@ -2515,10 +2590,12 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             a.scratch_dyn = 1;
         }
     }
-    cudaEvent_t e0, e1, e2;
-    MBE_CUDA_TRY(cudaEventCreate(&e0));
-    MBE_CUDA_TRY(cudaEventCreate(&e1));
-    MBE_CUDA_TRY(cudaEventCreate(&e2));
+    for (cudaEvent_t& e : eb.ev)
+        if (!e) MBE_CUDA_TRY(cudaEventCreate(&e));
+    cudaEvent_t e0 = eb.ev[0], e1 = eb.ev[1], e2 = eb.ev[2];
+    // a buffer that was (re)allocated since the last clean run starts unknown
+    if (eb.cmap.bytes < eb.cmap_clean) eb.cmap_clean = 0;
+    if (eb.ready.bytes < eb.ready_clean) eb.ready_clean = 0;
     float ms_a = 0, ms_b = 0;
     uint32_t chunks = 0;
     mbe_status result = MBE_OK;
@@ -2533,7 +2610,11 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         a.pool = (uint32_t*)eb.pool.ptr;
         a.pool_words = pool_words;
         a.pool_watermark = cfg.chunk_words ? std::min<uint64_t>(cfg.chunk_words, pool_words / 2) : pool_words / 2;
-        MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));  // kernels restore -1 after each root
+        if (eb.cmap_clean < cmap_bytes) {  // the kernels restore -1 after each root
+            MBE_CUDA_TRY(cudaMemsetAsync(eb.cmap.ptr, 0xFF, cmap_bytes, s));
+            eb.cmap_clean = cmap_bytes;
+        }
+        const size_t cmap_known = eb.cmap_clean;
         MBE_CUDA_TRY(cudaMemsetAsync(eb.results.ptr, 0, sizeof(ResultAcc) * ng, s));
         if (cfg.emit) MBE_CUDA_TRY(cudaMemsetAsync(cfg.emit->ctl, 0, 3 * sizeof(unsigned long long), s));
         ms_a = ms_b = 0;
@@ -2564,7 +2645,15 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             a.roots = list;
             a.n_roots = list_n;
             MBE_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
-            MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
+            if (eb.ready_clean < sizeof(uint32_t) * (size_t)task_cap) {
+                MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
+                eb.ready_clean = sizeof(uint32_t) * (size_t)task_cap;
+            }
+            // unknown while the kernels run; clean again only after a chunk
+            // that ended without an error
+            const size_t ready_known = eb.ready_clean;
+            eb.ready_clean = 0;
+            eb.cmap_clean = 0;
             MBE_CUDA_TRY(cudaEventRecord(e0, s));
             expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
             MBE_CUDA_TRY(cudaGetLastError());
@@ -2605,6 +2694,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             cudaEventElapsedTime(&t2, e1, e2);
             ms_a += t1;
             ms_b += t2;
+            if (!hc.error) {
+                eb.ready_clean = ready_known;
+                eb.cmap_clean = cmap_known;
+            }
             if (hc.error) {
                 static const char* names[] = {"none",
                                               "node pool exhausted",
@@ -2647,7 +2740,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         if (pool_exhausted && !cfg.pool_words) {
             size_t fr = 0, tt = 0;
             MBE_CUDA_TRY(cudaMemGetInfo(&fr, &tt));
-            uint64_t limit_words = (uint64_t)((fr + eb.pool.bytes) * 0.60) / 4;
+            uint64_t limit_words = std::min<uint64_t>((uint64_t)((fr + eb.pool.bytes) * 0.60) / 4, pool_cap_words);
             if (eb.pool_words * 2 <= limit_words) {
                 eb.pool_words *= 2;
                 continue;
@@ -2655,10 +2748,11 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         }
         break;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(e2);
-    if (result != MBE_OK) return result;
+    if (result != MBE_OK) {
+        // an error can stop the kernels with tasks still queued in the ring
+        eb.ready_clean = 0;
+        return result;
+    }
     if (!results_with_ctrl) {
         MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
         io->d2h += sizeof(ResultAcc) * ng;

@@ -25,7 +25,15 @@ struct EngineBuffers {
     // sizes chosen at first use from the device's free memory
     uint32_t arena_words = 0;
     uint64_t pool_words = 0;
+    // State the kernels leave behind: after a run that ended without an
+    // error every candidate-map entry is -1 again (each root restores what
+    // it touched) and every task-ring flag is 0 (every pushed task was
+    // taken).  Bytes known to be in that state, so they need no clearing.
+    size_t cmap_clean = 0;
+    size_t ready_clean = 0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // timing events, created once
     void release();
+    size_t bytes() const;  // device memory held
 };
 
 // Device buffers of the output stream (MBE_OPT_EMIT), owned by the caller
@@ -49,9 +57,14 @@ struct EngineConfig {
     uint32_t arena_words = 0;           // per warp; 0 = engine default
     uint64_t pool_words = 0;            // node pool cap; 0 = engine default (grows on demand)
     uint64_t chunk_words = 0;           // root records per chunk; 0 = half the pool
+    uint32_t solve_rows = 32;           // packed records with at most this many rows (<= 32) use the register search
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
     unsigned long long timeout_ns = 60ull * 1000000000ull;
     const EmitTarget* emit = nullptr;
+    // Bytes of device memory the run's buffers may hold in total (0 = no
+    // cap): arenas shrink to at most a quarter of it, the node pool gets
+    // what the other buffers leave and never grows past it.
+    uint64_t mem_cap = 0;
 };
 
 struct EngineStats {
@@ -66,9 +79,20 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                       std::vector<ResultAcc>& results, EngineStats* stats, IoCounters* io);
 
 // Enumeration of resident graphs with opts applied (capi.cu).
+// Engine knobs an autotuner sets for a group of graphs (0 = default).
+struct BatchKnobs {
+    uint32_t blocks_per_sm = 0;
+    uint32_t donate_min = 0;
+    uint32_t solve_rows = 32;
+    uint64_t chunk_words = 0;
+};
+
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
                     mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
-                    const EmitTarget* emit = nullptr);
+                    const EmitTarget* emit = nullptr, uint64_t mem_cap = 0, const BatchKnobs* knobs = nullptr);
+
+// Resident DFS blocks per SM on device dev (the launch's upper bound).
+cudaError_t dfs_blocks_per_sm(int dev, int* occ);
 
 // Raw launchers of the two enumeration kernels (root expansion: 256 threads
 // per block; DFS: kDfsWarps warps per block).

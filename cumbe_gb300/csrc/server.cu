@@ -6,10 +6,18 @@
 // so launches of different slots share the GPU at the same time.  A slot
 // that becomes free takes, under the queue lock, the oldest waiting request
 // and every later waiting request with the same thresholds (the engine
-// applies one threshold pair per launch) up to max_batch, as long as the
-// estimated search memory of everything admitted stays within mem_budget;
+// applies one threshold pair per launch) up to max_batch, while the
+// estimated search memory of the batch fits the slot's node-pool share;
 // requests arriving while others run join the next batch of the next free
 // slot.  Latency = done - submit on one steady clock.
+//
+// Memory: mem_budget is divided among the slots up front.  A slot's engine
+// buffers (node pool, per-warp arenas, scratch, task ring, root-expansion
+// maps) never hold more than its share: the arenas shrink to fit, the pool
+// gets what the other buffers leave and stops growing at the share, and a
+// batch larger than the pool is enumerated in root chunks that fit.  So the
+// search memory the server holds is bounded by mem_budget whatever the
+// requests; mbe_server_memory reports what it holds.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -79,11 +87,15 @@ struct mbe_server {
     int n_sm = 0;
     std::deque<DeviceGraph> graphs;      // stable addresses
     std::vector<uint64_t> graph_est;
-    std::mutex mu;                       // queue, results, admission
+    uint64_t graph_bytes = 0;            // device bytes of the resident graphs
+    uint64_t slot_cap = 0;               // device bytes one slot's engine buffers may hold
+    std::mutex mu;                       // queue, results, admission, memory figures
     std::condition_variable cv;
     std::deque<Req> queue;
     std::deque<mbe_request_result> done;
-    uint64_t inflight_bytes = 0;
+    std::vector<uint64_t> slot_bytes;    // device bytes each slot holds (after its last launch)
+    std::vector<uint32_t> slot_warm;     // warm-up epoch each slot has completed
+    uint32_t warm_epoch = 0;
     uint64_t next_id = 1;
     bool stopping = false;
     std::vector<std::thread> workers;
@@ -95,31 +107,60 @@ struct mbe_server {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
 
+    // Sizes a slot's buffers for every resident graph at once (largest
+    // side, widest row, all roots in one task ring) without expanding any
+    // root (thresholds no root meets), so that requests do not pay for
+    // device allocations and the synchronisation they cause.
+    void warm(uint32_t slot, EngineBuffers& eb, cudaStream_t stream, IoCounters& io) {
+        std::vector<const DeviceGraph*> devs;
+        {
+            std::lock_guard<std::mutex> glk(graph_mu);
+            for (const DeviceGraph& d : graphs) devs.push_back(&d);
+        }
+        if (!devs.empty()) {
+            mbe_opts opts;
+            std::memset(&opts, 0, sizeof opts);
+            opts.min_rows = opts.min_cols = 0xFFFFFFFFu;
+            opts.blocks_per_sm = cfg.blocks_per_sm;
+            std::vector<ResultAcc> acc;
+            EngineStats stats;
+            run_devs(eb, stream, &io, devs, (mbe_variant)cfg.variant, &opts, acc, stats, nullptr, slot_cap);
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        slot_bytes[slot] = eb.bytes();
+    }
+
     void worker(uint32_t slot) {
         cudaSetDevice(device);
         cudaStream_t stream = nullptr;
         cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
         EngineBuffers eb;
         IoCounters io;
+        // a batch's estimated root-record bytes should fit half the slot's
+        // share (the node pool); a request larger than that runs alone
+        const uint64_t batch_bytes = slot_cap / 2;
         for (;;) {
             std::vector<Req> batch;
+            bool do_warm = false;
+            uint32_t epoch = 0;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
+                    if (slot_warm[slot] != warm_epoch) {
+                        do_warm = true;
+                        epoch = warm_epoch;
+                        break;
+                    }
                     if (queue.empty()) {
                         if (stopping) break;
                         cv.wait(lk);
                         continue;
                     }
                     const Req& r0 = queue.front();
-                    if (inflight_bytes > 0 && inflight_bytes + r0.est > cfg.mem_budget) {
-                        cv.wait(lk);  // memory frees when another slot finishes
-                        continue;
-                    }
                     uint64_t admitted = 0;
                     for (auto it = queue.begin(); it != queue.end() && batch.size() < cfg.max_batch;) {
                         bool same = it->min_rows == r0.min_rows && it->min_cols == r0.min_cols;
-                        bool fits = batch.empty() || inflight_bytes + admitted + it->est <= cfg.mem_budget;
+                        bool fits = batch.empty() || admitted + it->est <= batch_bytes;
                         if (same && fits) {
                             admitted += it->est;
                             batch.push_back(*it);
@@ -128,10 +169,16 @@ struct mbe_server {
                             ++it;
                         }
                     }
-                    inflight_bytes += admitted;
                     break;
                 }
-                if (batch.empty()) break;  // stopping and drained
+                if (!do_warm && batch.empty()) break;  // stopping and drained
+            }
+            if (do_warm) {
+                warm(slot, eb, stream, io);
+                std::lock_guard<std::mutex> lk(mu);
+                slot_warm[slot] = epoch;
+                cv.notify_all();
+                continue;
             }
             double t_start = now();
             std::vector<const DeviceGraph*> devs;
@@ -146,10 +193,11 @@ struct mbe_server {
             opts.blocks_per_sm = cfg.blocks_per_sm;
             std::vector<ResultAcc> acc;
             EngineStats stats;
-            mbe_status st = run_devs(eb, stream, &io, devs, (mbe_variant)cfg.variant, &opts, acc, stats);
+            mbe_status st = run_devs(eb, stream, &io, devs, (mbe_variant)cfg.variant, &opts, acc, stats, nullptr,
+                                     slot_cap);
             double t_done = now();
             std::lock_guard<std::mutex> lk(mu);
-            uint64_t freed = 0;
+            slot_bytes[slot] = eb.bytes();
             for (size_t i = 0; i < batch.size(); i++) {
                 mbe_request_result rr;
                 std::memset(&rr, 0, sizeof rr);
@@ -164,9 +212,7 @@ struct mbe_server {
                 rr.batch_size = (uint32_t)batch.size();
                 rr.slot = slot;
                 done.push_back(rr);
-                freed += batch[i].est;
             }
-            inflight_bytes -= freed;
             cv.notify_all();
         }
         cudaStreamSynchronize(stream);
@@ -192,9 +238,15 @@ extern "C" mbe_status mbe_server_start(int device, const mbe_server_config* cfg,
     if (!s->cfg.slots) s->cfg.slots = 2;
     if (!s->cfg.max_batch) s->cfg.max_batch = 256;
     if (!s->cfg.mem_budget) s->cfg.mem_budget = 120ull << 30;
-    if (!cfg) s->cfg.blocks_per_sm = 2;
+    if (!cfg) s->cfg.blocks_per_sm = 3;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, device);
+    // each slot's share of the budget, and of 85% of the memory free now
+    size_t free_b = 0, tot_b = 0;
+    cudaMemGetInfo(&free_b, &tot_b);
+    s->slot_cap = std::min<uint64_t>(s->cfg.mem_budget, (uint64_t)(free_b * 0.85)) / s->cfg.slots;
+    s->slot_bytes.assign(s->cfg.slots, 0);
+    s->slot_warm.assign(s->cfg.slots, 0);
     if (cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete s;
         return fail(MBE_ERR_CUDA, "cudaStreamCreate failed");
@@ -212,11 +264,41 @@ extern "C" mbe_status mbe_server_add_graph(mbe_server* s, const mbe_graph* g, ui
     mbe_status st = build_device_graph(g, s->upload_stream, s->n_sm, &d, &s->io_upload);
     if (st != MBE_OK) return st;
     uint64_t est = estimate_bytes(g);
+    const uint64_t gbytes = 4ull * (d.nR + 1) + 4ull * (d.nL + 1) + 8ull * d.nE + 12ull * d.nR + 8ull * d.nL;
     std::lock_guard<std::mutex> glk(s->graph_mu);
     *graph_id = (uint32_t)s->graphs.size();
     s->graphs.push_back(std::move(d));
     std::lock_guard<std::mutex> lk(s->mu);
     s->graph_est.push_back(est);
+    s->graph_bytes += gbytes;
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_server_warmup(mbe_server* s) {
+    clear_error();
+    if (!s) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->stopping) return fail(MBE_ERR_BUSY, "server is stopping");
+    const uint32_t epoch = ++s->warm_epoch;
+    s->cv.notify_all();
+    s->cv.wait(lk, [&] {
+        for (uint32_t w : s->slot_warm)
+            if (w != epoch) return false;
+        return true;
+    });
+    return MBE_OK;
+}
+
+extern "C" mbe_status mbe_server_memory(mbe_server* s, uint64_t* search_bytes, uint64_t* graph_bytes,
+                                        uint64_t* slot_cap) {
+    clear_error();
+    if (!s) return fail(MBE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint64_t t = 0;
+    for (uint64_t b : s->slot_bytes) t += b;
+    if (search_bytes) *search_bytes = t;
+    if (graph_bytes) *graph_bytes = s->graph_bytes;
+    if (slot_cap) *slot_cap = s->slot_cap;
     return MBE_OK;
 }
 

@@ -6,6 +6,8 @@
                        degree cap 7,500, seed 2 (the headline workload).
   power_law_1400k_500k 1.4M x 500k, 8M edges, gamma 1.9, plus 200 planted
                        K_{20,30} blocks at density 0.9 over hubs (stress).
+  stress_params(k)     the stress shape at 1/k of its size.
+  served_pool()        the served workload's pool (from the four above).
   batch_4096           4,096 independent uniform random bipartite graphs,
                        graph s: |U| log-uniform in [50, 5000], |V| = |U|/2,
                        density log-uniform in [0.002, 0.05], parameters
@@ -29,6 +31,29 @@ SINGLE = {
                                  max_deg=0, seed=3, planted=200, planted_rows=20, planted_cols=30,
                                  planted_density=0.9),
 }
+
+
+def stress_params(scale: int) -> dict:
+    """The load-imbalance stress graph's shape (power_law_1400k_500k) at
+    1/scale of its size: sides and edges divided by scale, 200/scale
+    planted K_{20,30} blocks (at least one)."""
+    full = SINGLE["power_law_1400k_500k"]
+    return dict(full, n_rows=full["n_rows"] // scale, n_cols=full["n_cols"] // scale,
+                n_edges=full["n_edges"] // scale, planted=max(1, round(full["planted"] / scale)))
+
+
+def served_pool() -> list[tuple[str, dict]]:
+    """The served workload's graph pool, drawn from the four other
+    workloads: the 2,000 x 1,000 graph, the 94,000 x 30,000 graph, the
+    stress shape at 1/250 and 1/100 of its size, and the batch graphs with
+    |U| <= 1000 (the larger batch graphs are left out so that 2,000
+    requests/s stay within what one GPU serves)."""
+    pool = [("power_law_2k_1k", SINGLE["power_law_2k_1k"]),
+            ("power_law_94k_30k", SINGLE["power_law_94k_30k"]),
+            ("stress_1_250", stress_params(250)),
+            ("stress_1_100", stress_params(100))]
+    pool += [("batch", p) for p in batch(4096) if p["n_rows"] <= 1000]
+    return pool
 
 
 def batch_params(seed: int) -> dict:

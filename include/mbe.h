@@ -258,6 +258,39 @@ MBE_API mbe_status mbe_batch_run(mbe_ctx* ctx, const mbe_graph* const* graphs, u
                          mbe_variant variant, const mbe_opts* opts,
                          mbe_result* out, float* total_ms);
 
+/* ---- batched mode: autotuning ------------------------------------------ */
+
+/* One size bucket's tuning.  No reference counterpart (the reference has one
+ * fixed launch shape, src/main.cu:50-63).  A graph's bucket is
+ * 4 * (|R| class) + (degree class), with |R| the branching side's vertices
+ * with edges (classes < 256, < 1024, < 4096, larger) and the degree E/|R|
+ * (classes < 4, < 16, < 64, larger). */
+typedef struct mbe_tune_choice {
+    uint32_t bucket;
+    uint32_t n_graphs;           /* graphs of the tuned batch in the bucket  */
+    uint32_t sample_graphs;      /* graphs the sweep timed                   */
+    uint32_t blocks_per_sm;      /* DFS blocks per SM (0 = all that fit)     */
+    uint32_t donate_min;         /* donation granularity (0 = default 2)     */
+    uint32_t solve_rows;         /* register-search row limit (0 = off)      */
+    uint32_t chunk_mwords;       /* root records per chunk, Mi 32-bit words  */
+    uint32_t trials;             /* configurations timed                     */
+    float ms_default;            /* the sample's device time, defaults       */
+    float ms_tuned;              /* ... with this choice                     */
+} mbe_tune_choice;
+
+/* Tunes the engine for the buckets of the graphs given: for each bucket, a
+ * sample of its graphs (up to 32, spread over its edge counts) is timed
+ * with CUDA events under a coordinate descent over DFS blocks per SM,
+ * donation granularity, register-search row limit and root chunk size (a
+ * change is kept when it is 3% faster).  The choices are cached for the
+ * process per (device, variant, bucket); mbe_batch_run then runs each group
+ * of graphs that share a choice as one launch pair with it (when opts sets
+ * no tuning field itself).  Up to cap choices are written to out. */
+MBE_API mbe_status mbe_batch_tune(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n, mbe_variant variant,
+                                  const mbe_opts* opts, mbe_tune_choice* out, uint32_t cap, uint32_t* n_out);
+/* Forgets the cached choices of ctx's device. */
+MBE_API mbe_status mbe_batch_tune_reset(mbe_ctx* ctx);
+
 /* Canonical per-biclique hash: rows A and cols B in file orientation, in
  * any order.  The graph hash is the wrapping sum of this over bicliques. */
 MBE_API uint64_t mbe_biclique_hash(const uint32_t* rows, uint32_t n_rows,
@@ -277,14 +310,17 @@ MBE_API mbe_variant mbe_variant_from_name(const char* name);
  * GPU (`blocks_per_sm` DFS blocks per SM), so batches of different slots
  * overlap on the device.  A free slot takes the oldest waiting request
  * plus every later waiting request with the same thresholds, up to
- * `max_batch`, while the estimated search memory of admitted requests stays
- * within `mem_budget` bytes (a request larger than the budget runs alone). */
+ * `max_batch`, while the estimated root-record memory of the batch fits
+ * half the slot's share of `mem_budget` (a larger request runs alone).
+ * `mem_budget` bounds the device memory of the search: it is divided among
+ * the slots up front, and a slot's buffers never outgrow its share (its
+ * node pool stops growing there and larger work runs in root chunks). */
 typedef struct mbe_server mbe_server;
 
 typedef struct mbe_server_config {
     uint32_t slots;              /* default 2                               */
     uint32_t max_batch;          /* default 256 (1 = one request per launch) */
-    uint32_t blocks_per_sm;      /* default 2; 0 = the whole GPU per slot   */
+    uint32_t blocks_per_sm;      /* default 3; 0 = the whole GPU per slot   */
     uint32_t variant;            /* mbe_variant                             */
     uint64_t mem_budget;         /* default 120 GB                          */
 } mbe_server_config;
@@ -312,6 +348,17 @@ MBE_API mbe_status mbe_server_submit(mbe_server* s, uint32_t graph_id, uint32_t 
 MBE_API mbe_status mbe_server_poll(mbe_server* s, mbe_request_result* out, uint32_t cap, uint32_t* n_out);
 /* Seconds since the server started (the clock of mbe_request_result). */
 MBE_API double mbe_server_clock(mbe_server* s);
+/* Sizes every slot's device buffers for the graphs added so far and
+ * returns when all slots are done, so that the requests that follow pay for
+ * no device allocation (cudaMalloc and cudaFree synchronise the device, which
+ * would stall the other slots' work). */
+MBE_API mbe_status mbe_server_warmup(mbe_server* s);
+/* Device memory the server holds: search_bytes = the slots' engine buffers
+ * (never above mem_budget: each slot holds at most slot_cap =
+ * min(mem_budget, 85% of the memory free at start) / slots), graph_bytes =
+ * the resident graphs. */
+MBE_API mbe_status mbe_server_memory(mbe_server* s, uint64_t* search_bytes, uint64_t* graph_bytes,
+                                     uint64_t* slot_cap);
 /* Finishes every queued request, stops the workers and frees the server. */
 MBE_API mbe_status mbe_server_stop(mbe_server* s);
 

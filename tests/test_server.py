@@ -52,3 +52,35 @@ def test_results_same_alone_and_in_the_mix(engine, slots, max_batch):
         assert got["done_s"] >= got["start_s"] >= got["submit_s"]
     if max_batch > 1:
         assert max(r["batch_size"] for r in res.values()) > 1  # requests were batched
+
+
+def test_memory_budget_bounds_what_the_server_holds(engine):
+    """mem_budget is divided among the slots up front; after warm-up and a
+    stream of requests (the 2,000 x 1,000 graph and batch graphs) the slots'
+    device buffers stay within it, and every result is still exact."""
+    rng = np.random.default_rng(5)
+    graphs = [cm.Graph.generate(**workloads.batch_params(s)) for s in range(40)
+              if workloads.batch_params(s)["n_rows"] <= 2000]
+    graphs.append(cm.Graph.generate(**workloads.SINGLE["power_law_2k_1k"]))
+    budget = 3 << 30
+    srv = cm.Server(0, slots=2, max_batch=64, mem_budget=budget)
+    try:
+        gids = [srv.add_graph(g) for g in graphs]
+        srv.warmup()
+        warm = srv.memory()
+        assert warm["slot_cap"] == budget // 2
+        assert 0 < warm["search_bytes"] <= budget
+        reqs = []
+        for _ in range(80):
+            k = int(rng.integers(len(gids)))
+            reqs.append((srv.submit(gids[k]), k))
+        res = {r["request"]: r for r in _drain(srv, len(reqs))}
+        after = srv.memory()
+    finally:
+        srv.stop()
+    assert after["search_bytes"] <= budget
+    assert after["graph_bytes"] > 0
+    for rid, k in reqs:
+        want = engine.enumerate(graphs[k])
+        assert res[rid]["status"] == 0
+        assert (res[rid]["count"], res[rid]["hash"]) == (want.count, want.hash)
