@@ -290,6 +290,16 @@ def served_leg(rate=2000.0, n_requests=8000, seed=11):
         finally:
             srv.stop()
         lat = np.array([r["done_s"] - r["submit_s"] for r in out]) * 1e3
+        by_req = {r["request"]: r for r in out}
+        classes = {}
+        for k, rid in enumerate(sorted(by_req)):  # request ids follow submission order
+            classes.setdefault(names[picks[k]], []).append(by_req[rid])
+        per_class = {name: {"n": len(rs),
+                            "p50_ms": float(np.percentile([(r["done_s"] - r["submit_s"]) * 1e3 for r in rs], 50)),
+                            "p99_ms": float(np.percentile([(r["done_s"] - r["submit_s"]) * 1e3 for r in rs], 99)),
+                            "wait_p99_ms": float(np.percentile([(r["start_s"] - r["submit_s"]) * 1e3 for r in rs], 99)),
+                            "service_p50_ms": float(np.percentile([(r["done_s"] - r["start_s"]) * 1e3 for r in rs], 50))}
+                     for name, rs in classes.items()}
         span = max(r["done_s"] for r in out) - min(r["submit_s"] for r in out)
         tot = sum(r["count"] for r in out)
         ok = all(r["status"] == 0 for r in out)
@@ -297,7 +307,7 @@ def served_leg(rate=2000.0, n_requests=8000, seed=11):
         return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "max_ms": float(lat.max()), "requests_per_s": n_requests / span, "bicliques_per_s": tot / span,
                 "all_ok": ok, "mean_batch": float(np.mean([r["batch_size"] for r in out])),
-                "search_bytes": mem["search_bytes"], "graph_bytes": mem["graph_bytes"]}, res
+                "search_bytes": mem["search_bytes"], "graph_bytes": mem["graph_bytes"], "per_class": per_class}, res
 
     cont, r1 = run(2, 256, 3)
     plain, r2 = run(1, 1, 0)
@@ -309,20 +319,45 @@ def served_leg(rate=2000.0, n_requests=8000, seed=11):
                     "1/250 and 1/100, and the batch graphs with |U| <= 1000"}
 
 
+# Root sample of the full-size stress graph the bench times: every 10th
+# root among the first 411,000 positions of the processing order (degree
+# ascending; 457,386 roots have edges, and these reach degree 18).  The hub
+# roots beyond carry the graph's explosive part (more than 10^12 maximal
+# bicliques in all), which no engine enumerates.
+STRESS_SAMPLE = dict(root_begin=0, root_end=411000, root_stride=10)
+
+
 def stress_leg(eng):
-    """The load-imbalance stress graph's shape (Chung-Lu gamma 1.9 on both
-    sides, uncapped, planted K_{20,30} blocks at density 0.9 over hubs) at
-    1/50 of its size: its full size has far more maximal bicliques than any
-    engine can enumerate (the count grows ~40x per doubling of the graph)."""
+    """The load-imbalance stress graph at its stated size (1.4M x 500k, 8M
+    Chung-Lu edges, gamma 1.9 uncapped, 200 planted K_{20,30} blocks at
+    density 0.9 over hubs) on a fixed root sample (STRESS_SAMPLE), and its
+    shape at 1/50 of the size enumerated in full."""
     import cumbe_gb300 as cm
-    p = dict(n_rows=28000, n_cols=10000, n_edges=160000, gamma_rows=1.9, gamma_cols=1.9, max_deg=0, seed=3,
-             planted=4, planted_rows=20, planted_cols=30, planted_density=0.9)
-    g = cm.Graph.generate(**p)
-    eng.enumerate(cm.Graph.generate(**dict(p, n_rows=14000, n_cols=5000, n_edges=80000, planted=2)))  # warm-up
-    r = eng.enumerate(g)
+    from cumbe_gb300 import workloads
+    p_full = workloads.SINGLE["power_law_1400k_500k"]
+    t0 = time.perf_counter()
+    g = cm.Graph.generate(**p_full)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    eng.upload(g)  # H2D, transpose, root order on the device
+    upload_s = time.perf_counter() - t0
+    eng.enumerate(g, root_begin=0, root_end=1000, root_stride=10)  # warm-up
+    r = eng.enumerate(g, **STRESS_SAMPLE)
     eng.release(g)
-    return {"workload": "stress shape at 1/50 scale", **p, "bicliques": r.count, "hash": f"{r.hash:#018x}",
-            "ms": r.ms, "bicliques_per_s": r.count / (r.ms / 1e3)}
+    full = {"workload": "power_law_1400k_500k (stated size)", **p_full, "n_edges_distinct": g.info()["n_edges"],
+            "root_sample": STRESS_SAMPLE, "roots_sampled": len(range(0, 411000, 10)),
+            "bicliques": r.count, "hash": f"{r.hash:#018x}", "tree_nodes": r.nodes, "ms": r.ms,
+            "bicliques_per_s": r.count / (r.ms / 1e3) if r.ms > 0 else None,
+            "tree_nodes_per_s": r.nodes / (r.ms / 1e3) if r.ms > 0 else None,
+            "generate_s": gen_s, "upload_transpose_s": upload_s}
+    p = workloads.stress_params(50)
+    gs = cm.Graph.generate(**p)
+    eng.enumerate(cm.Graph.generate(**workloads.stress_params(100)))  # warm-up
+    rs = eng.enumerate(gs)
+    eng.release(gs)
+    scaled = {"workload": "stress shape at 1/50 scale, full enumeration", **p, "bicliques": rs.count,
+              "hash": f"{rs.hash:#018x}", "ms": rs.ms, "bicliques_per_s": rs.count / (rs.ms / 1e3)}
+    return {"full_size_sample": full, "scaled_full": scaled}
 
 
 def run_reference(args, wl, rank, world):

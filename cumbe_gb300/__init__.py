@@ -77,7 +77,7 @@ class _TuneChoice(ctypes.Structure):
 
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
-                ("variant", ctypes.c_uint32), ("mem_budget", ctypes.c_uint64)]
+                ("variant", ctypes.c_uint32), ("mem_budget", ctypes.c_uint64), ("heavy_bytes", ctypes.c_uint64)]
 
 
 class _RequestResult(ctypes.Structure):
@@ -397,8 +397,8 @@ class Server:
     finished ones with their timestamps on the server clock."""
 
     def __init__(self, device: int = 0, slots: int = 2, max_batch: int = 256, blocks_per_sm: int = 3,
-                 variant: str = "cuMBE", mem_budget: int = 0):
-        cfg = _ServerConfig(slots, max_batch, blocks_per_sm, VARIANTS[variant], mem_budget)
+                 variant: str = "cuMBE", mem_budget: int = 0, heavy_bytes: int = 0):
+        cfg = _ServerConfig(slots, max_batch, blocks_per_sm, VARIANTS[variant], mem_budget, heavy_bytes)
         self._h = _VP()
         _check(lib().mbe_server_start(device, ctypes.byref(cfg), ctypes.byref(self._h)), "mbe_server_start")
 

@@ -2485,6 +2485,13 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         pool_cap_words = ((cfg.mem_cap - fixed) / 4) & ~31ull;
         eb.pool_words = std::min<uint64_t>(eb.pool_words, pool_cap_words);
         if (eb.pool.bytes > sizeof(uint32_t) * pool_cap_words) eb.pool.free();  // reallocated below, smaller
+        // The scratch is allocated for its bound now (it is counted in the
+        // cap anyway), not grown per chunk: a capped context serves requests
+        // next to other streams, and growing a buffer (cudaFree) would wait
+        // for every kernel on the device, theirs included.
+        mbe_status sst = eb.scratch.ensure(sizeof(uint32_t) * (size_t)nwarpsB *
+                                           scratch_words(maxW, scr_b, kc_b, cfg.emit != nullptr));
+        if (sst) return sst;
     }
 
     mbe_status st;

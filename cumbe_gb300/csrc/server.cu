@@ -9,7 +9,9 @@
 // applies one threshold pair per launch) up to max_batch, while the
 // estimated search memory of the batch fits the slot's node-pool share;
 // requests arriving while others run join the next batch of the next free
-// slot.  Latency = done - submit on one steady clock.
+// slot.  Heavy requests (estimated search memory above heavy_bytes) are
+// taken by slot 0 only and run alone, so the other slots always serve the
+// light ones.  Latency = done - submit on one steady clock.
 //
 // Memory: mem_budget is divided among the slots up front.  A slot's engine
 // buffers (node pool, per-warp arenas, scratch, task ring, root-expansion
@@ -139,6 +141,12 @@ struct mbe_server {
         // a batch's estimated root-record bytes should fit half the slot's
         // share (the node pool); a request larger than that runs alone
         const uint64_t batch_bytes = slot_cap / 2;
+        // Heavy requests (estimated search memory above heavy_bytes) run on
+        // slot 0 only, one per launch: the other slots keep serving light
+        // requests while a heavy one holds slot 0, so light requests never
+        // queue behind heavy ones (with one slot, everything shares it).
+        const uint64_t heavy = cfg.heavy_bytes;
+        const bool light_only = slot > 0;
         for (;;) {
             std::vector<Req> batch;
             bool do_warm = false;
@@ -151,15 +159,21 @@ struct mbe_server {
                         epoch = warm_epoch;
                         break;
                     }
-                    if (queue.empty()) {
-                        if (stopping) break;
+                    // the oldest request this slot may take: slot 0 any,
+                    // the others light ones only
+                    auto first = queue.begin();
+                    while (first != queue.end() && light_only && first->est > heavy) ++first;
+                    if (first == queue.end()) {
+                        if (stopping && queue.empty()) break;
                         cv.wait(lk);
                         continue;
                     }
-                    const Req& r0 = queue.front();
+                    const Req r0 = *first;
+                    const bool r0_heavy = r0.est > heavy;
                     uint64_t admitted = 0;
-                    for (auto it = queue.begin(); it != queue.end() && batch.size() < cfg.max_batch;) {
-                        bool same = it->min_rows == r0.min_rows && it->min_cols == r0.min_cols;
+                    for (auto it = first; it != queue.end() && batch.size() < cfg.max_batch;) {
+                        bool same = it->min_rows == r0.min_rows && it->min_cols == r0.min_cols &&
+                                    (it->est > heavy) == r0_heavy && (batch.empty() || !r0_heavy);
                         bool fits = batch.empty() || admitted + it->est <= batch_bytes;
                         if (same && fits) {
                             admitted += it->est;
@@ -238,6 +252,7 @@ extern "C" mbe_status mbe_server_start(int device, const mbe_server_config* cfg,
     if (!s->cfg.slots) s->cfg.slots = 2;
     if (!s->cfg.max_batch) s->cfg.max_batch = 256;
     if (!s->cfg.mem_budget) s->cfg.mem_budget = 120ull << 30;
+    if (!s->cfg.heavy_bytes) s->cfg.heavy_bytes = 32ull << 20;
     if (!cfg) s->cfg.blocks_per_sm = 3;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, device);

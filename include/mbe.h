@@ -323,6 +323,9 @@ typedef struct mbe_server_config {
     uint32_t blocks_per_sm;      /* default 3; 0 = the whole GPU per slot   */
     uint32_t variant;            /* mbe_variant                             */
     uint64_t mem_budget;         /* default 120 GB                          */
+    uint64_t heavy_bytes;        /* requests whose estimated search memory
+                                    exceeds this run on slot 0 only, alone
+                                    (default 32 MiB)                        */
 } mbe_server_config;
 
 typedef struct mbe_request_result {

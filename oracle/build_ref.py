@@ -22,7 +22,9 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_ROOT = "/root/reference"
+# where the reference's sources are: MBE_REFERENCE_ROOT, else the read-only
+# checkout this recipe was written against
+REF_ROOT = os.environ.get("MBE_REFERENCE_ROOT", "/root/reference")
 CUBIN = os.path.join(OUT, "cumbe_ref.cubin")
 RUNNER = os.path.join(OUT, "ref_runner")
 GEN_BI = os.path.join(OUT, "gen_bi")

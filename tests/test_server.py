@@ -84,3 +84,31 @@ def test_memory_budget_bounds_what_the_server_holds(engine):
         want = engine.enumerate(graphs[k])
         assert res[rid]["status"] == 0
         assert (res[rid]["count"], res[rid]["hash"]) == (want.count, want.hash)
+
+
+def test_heavy_requests_run_alone_on_slot_0(engine):
+    """With heavy_bytes below the 2,000 x 1,000 graph's estimate (~5.9 MB)
+    its requests count as heavy: they run on slot 0 only, one per launch,
+    while the light batch graphs keep being served and batched."""
+    rng = np.random.default_rng(9)
+    light = [cm.Graph.generate(**workloads.batch_params(s)) for s in range(12)
+             if workloads.batch_params(s)["n_rows"] <= 800]
+    heavy = cm.Graph.generate(**workloads.SINGLE["power_law_2k_1k"])
+    graphs = light + [heavy]
+    srv = cm.Server(0, slots=3, max_batch=64, heavy_bytes=1 << 20)
+    try:
+        gids = [srv.add_graph(g) for g in graphs]
+        assert srv.estimate(gids[-1]) > (1 << 20) >= max(srv.estimate(g) for g in gids[:-1])
+        reqs = []
+        for i in range(120):
+            k = len(graphs) - 1 if i % 10 == 0 else int(rng.integers(len(light)))
+            reqs.append((srv.submit(gids[k]), k))
+        res = {r["request"]: r for r in _drain(srv, len(reqs))}
+    finally:
+        srv.stop()
+    for rid, k in reqs:
+        r = res[rid]
+        want = engine.enumerate(graphs[k])
+        assert r["status"] == 0 and (r["count"], r["hash"]) == (want.count, want.hash)
+        if k == len(graphs) - 1:
+            assert r["slot"] == 0 and r["batch_size"] == 1
