@@ -27,6 +27,7 @@ VARIANTS = {"cuMBE": 0, "noRS": 1, "noES": 2, "noWS": 3}
 OPT_NO_HASH = 1
 OPT_EMIT = 2
 OPT_TIMING = 4
+OPT_L2_PIN = 8
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "IO", 3: "FORMAT", 4: "CUDA", 5: "OUT_OF_MEMORY",
           6: "DEVICE_TIMEOUT", 7: "CAPACITY", 8: "NO_DEVICE", 9: "BUSY"}
@@ -316,7 +317,8 @@ class Engine:
         cols) tuples in file ids, with room for emit_cap bicliques and
         emit_ids_cap ids (default 64 per biclique); a run whose output does
         not fit raises, naming how many were written."""
-        flags = OPT_TIMING | (0 if hash else OPT_NO_HASH) | (OPT_EMIT if emit_cap else 0)
+        flags = OPT_TIMING | (0 if hash else OPT_NO_HASH) | (OPT_EMIT if emit_cap else 0) | \
+            (OPT_L2_PIN if tuning.pop("l2_pin", False) else 0)
         o = _opts(flags=flags, min_rows=min_rows, min_cols=min_cols, **tuning)
         if emit_cap:
             ids_cap = emit_ids_cap or 64 * emit_cap

@@ -62,6 +62,7 @@ EngineConfig make_config(mbe_variant v, const mbe_opts* o, bool swapped) {
         if (o->blocks_per_sm) c.blocks_per_sm = o->blocks_per_sm;
         if (o->stack_words) c.arena_words = (o->stack_words + 3u) & ~3u;
         if (o->wait_timeout_ns) c.timeout_ns = o->wait_timeout_ns;
+        c.l2_pin = (o->flags & MBE_OPT_L2_PIN) != 0;
     }
     if (const char* env = std::getenv("MBE_POOL_MB")) {
         unsigned long long mb = std::strtoull(env, nullptr, 10);

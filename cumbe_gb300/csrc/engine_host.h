@@ -58,6 +58,7 @@ struct EngineConfig {
     uint64_t pool_words = 0;            // node pool cap; 0 = engine default (grows on demand)
     uint64_t chunk_words = 0;           // root records per chunk; 0 = half the pool
     uint32_t solve_rows = 32;           // packed records with at most this many rows (<= 32) use the register search
+    bool l2_pin = false;                // single-graph, uncapped runs: keep the L-side adjacency persisting in L2
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
     unsigned long long timeout_ns = 60ull * 1000000000ull;
     const EmitTarget* emit = nullptr;

@@ -379,7 +379,7 @@ mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, Devi
     GD_TRY(cudaMalloc(&cursor, (size_t)nmax * 4 + 4));
     GD_TRY(cudaMalloc(&scan_tmp, exclusive_scan_tmp_words(nmax) * 4));
     GD_TRY(cudaMalloc(&d.r_ptr, ((size_t)d.nR + 1) * 4));
-    GD_TRY(cudaMalloc(&d.r_adj, ne1 * 4));
+    GD_TRY(cudaMalloc(&d.r_adj, (ne1 + kAdjSlack) * 4));
     GD_TRY(cudaMalloc(&d.l_ptr, ((size_t)d.nL + 1) * 4));
     GD_TRY(cudaMalloc(&d.l_adj, ne1 * 4));
     GD_TRY(cudaMalloc(&d.r_orig, ((size_t)d.nR + 1) * 4));

@@ -32,9 +32,14 @@ struct DeviceGraph {
     void release();
 };
 
+// Words allocated past the end of a device adjacency array, so that a copy
+// rounded out to 16-byte boundaries stays inside the allocation.
+constexpr uint32_t kAdjSlack = 4;
+
 // Flat view passed to kernels (by value).
 struct GraphView {
-    uint32_t nR, nL, swapped, pad;
+    uint32_t nR, nL, swapped;
+    uint32_t r_adj_slack;       // readable words allocated past r_adj[r_ptr[nR]] (for 16-byte bulk copies)
     const uint32_t* r_ptr;
     const uint32_t* r_adj;
     const uint32_t* l_ptr;
@@ -45,7 +50,7 @@ struct GraphView {
 };
 
 inline GraphView view_of(const DeviceGraph& d) {
-    return GraphView{d.nR, d.nL, d.swapped, 0, d.r_ptr, d.r_adj, d.l_ptr, d.l_adj, d.r_orig, d.eR, d.eL};
+    return GraphView{d.nR, d.nL, d.swapped, kAdjSlack, d.r_ptr, d.r_adj, d.l_ptr, d.l_adj, d.r_orig, d.eR, d.eL};
 }
 
 mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out, IoCounters* io);

@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY (the oracle's pin, never part of the product).
 //
-//   ref_runner <cumbe_ref.cubin> <graph.bi> [cuMBE|noRS|noES|noWS]
+//   ref_runner <cumbe_ref.cubin> <graph.bi> [cuMBE|noRS|noES|noWS] [device|managed]
 //
 // The cubin holds the reference's kernels compiled from its unmodified
 // sources (oracle/build_ref.py).  This program restates the reference's
@@ -15,7 +15,10 @@
 // (:190-199) and print the reference's own output lines (:207, :223).
 //
 // Differences, none of which changes what the kernels compute:
-//  - plain device memory instead of managed memory;
+//  - plain device memory instead of managed memory, unless the fifth
+//    argument is "managed" (then every buffer is managed memory, allocated
+//    with cuMemAllocManaged as src/main.cu allocates with cudaMallocManaged,
+//    and cleared as the operating system clears new pages);
 //  - CUDA_TRANSPOSE's two `long long*` size arguments get 8-byte buffers
 //    holding the sizes (the reference passes 4-byte ints there and relies
 //    on zero padding, src/main.cu:112-113 vs src/transpose.cuh:1);
@@ -47,9 +50,14 @@ struct Node {
     int start, length;
 };
 
+static bool g_managed = false;
+
 static CUdeviceptr dalloc(size_t bytes) {
     CUdeviceptr p;
-    CK(cuMemAlloc(&p, bytes ? bytes : 8));
+    if (g_managed)
+        CK(cuMemAllocManaged(&p, bytes ? bytes : 8, CU_MEM_ATTACH_GLOBAL));
+    else
+        CK(cuMemAlloc(&p, bytes ? bytes : 8));
     CK(cuMemsetD8(p, 0, bytes ? bytes : 8));
     return p;
 }
@@ -83,6 +91,7 @@ int main(int argc, char** argv) {
         return 2;
     }
     std::string algo = argc > 3 ? argv[3] : "cuMBE";
+    g_managed = argc > 4 && std::string(argv[4]) == "managed";
     algo = (algo == "noRS" || algo == "noES" || algo == "noWS") ? algo : "cuMBE";
 
     // .bi reader (src/main.cu:38-48)
@@ -207,7 +216,8 @@ int main(int argc, char** argv) {
     CK(cuMemcpyDtoH(&count, num_mb, sizeof(int)));
     std::printf("algorithm: %s\n|R|: %d, |L|: %d, |E|: %d\ngrid_size: %d, block_size: %d\n", algo.c_str(), NUM_R,
                 NUM_L, NUM_EDGES, numBlocks, numThreads);
-    std::printf("maximal bicliques: %d\nruntime (s): %g\n", count, ms / 1000.0);
+    std::printf("maximal bicliques: %d\nruntime (s): %g\nmemory: %s\n", count, ms / 1000.0,
+                g_managed ? "managed" : "device");
     CK(cuModuleUnload(mod));
     CK(cuDevicePrimaryCtxRelease(dev));
     return 0;

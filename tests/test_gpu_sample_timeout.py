@@ -81,3 +81,14 @@ def test_device_wait_timeout_is_an_error_status_and_the_context_recovers(engine)
     for _ in range(2):
         got = engine.enumerate(g)
         assert (got.count, got.hash) == (want.count, want.hash)
+
+
+def test_l2_persisting_window_gives_the_same_result(engine):
+    """MBE_OPT_L2_PIN (an access-policy window keeping the L-side adjacency
+    persisting in L2 for a one-graph run) changes no result, and the window
+    is cleared afterwards (a later plain run is exact too)."""
+    g = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)
+    want = oracle.ref_enumerate(*g.csr(), threads=4)
+    for pin in (True, False, True):
+        got = engine.enumerate(g, l2_pin=pin)
+        assert (got.count, got.hash) == (want.count, want.hash), pin
