@@ -846,9 +846,23 @@ __shared__ uint32_t s_Pos[kWarpsB][kShRows];      // their parent positions
 __shared__ unsigned long long s_Keys[kWarpsB][kShRows];  // P' keys of a packed child
 __shared__ SolveLevel s_Solve[kWarpsB][kSolveRows + 1];  // saved levels of the register search
 __shared__ GraphView s_G[kWarpsB];                // the graph of the warp's current task
+__shared__ ResultAcc s_acc[kWarpsB];              // the current task's counts (flushed per task)
 
 __device__ __forceinline__ uint32_t warp_in_block() { return threadIdx.x >> 5; }
 __device__ __forceinline__ WarpCtx& my_wc() { return s_wc[warp_in_block()]; }
+
+// Adds one evaluation's counts (kept in registers while it runs) to the
+// warp's accumulator in shared memory: lane 0 writes, so nothing of it stays
+// live in registers across the search loop's out-of-line calls.
+__device__ __forceinline__ void acc_commit(const ResultAcc& v) {
+    if (lane_id() == 0) {
+        ResultAcc& s = s_acc[warp_in_block()];
+        s.count += v.count;
+        s.hash += v.hash;
+        s.nodes += v.nodes;
+        s.words += v.words;
+    }
+}
 
 // Ticket queue: an idle warp takes the next slot index with one atomicAdd
 // and then watches only that slot's ready flag, so waiting warps never
@@ -1555,12 +1569,8 @@ __device__ __noinline__
 #else
 __device__
 #endif
-ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, uint32_t arena_top,
-                               ResultAcc& acc_out, bool replay, bool known_max) {
-    // a replayed evaluation re-derives a donated node: its counts belong to
-    // the donor and are discarded
-    ResultAcc scratch_acc{};
-    ResultAcc& acc = replay ? scratch_acc : acc_out;
+ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t* nd, uint32_t i, uint32_t arena_top,
+                         ResultAcc& acc, bool replay, bool known_max) {
     const unsigned lane = lane_id();
     const uint32_t wb = warp_in_block();
     WarpCtx& wc = my_wc();
@@ -1715,13 +1725,24 @@ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
     return out;
 }
 
+// eval_child_impl with its counts committed to the warp's accumulator; a
+// replayed evaluation re-derives a donated node, and its counts belong to
+// the donor: they are dropped.
+__device__ __forceinline__ ChildOut eval_child(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
+                                               uint32_t i, uint32_t arena_top, bool replay, bool known_max) {
+    ResultAcc acc{};
+    const ChildOut o = eval_child_impl(a, G, nd, i, arena_top, acc, replay, known_max);
+    if (!replay) acc_commit(acc);
+    return o;
+}
+
 // Maximality of up to 32 consecutive children of a record with one-word
 // rows, one lane per child: lane j takes child base + j and walks the rows
 // of Q u P[0..i) that can cover L_i, in order, until one does.  At every
 // step all lanes read the same row (one broadcast load), eight rows per
 // step.  Returns the children no row covers.  Exact: the same test
 // eval_child makes, skipping only rows whose count rules them out.
-__device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, ResultAcc& acc) {
+__device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb) {
     const unsigned lane = lane_id();
     const bool active = lane < nb;
     const uint32_t nq = R.nq;
@@ -1771,9 +1792,11 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb, R
             }
         }
     }
-    unsigned long long scanned = warp_sum((unsigned long long)seen);
-    acc.words += scanned + nb;
-    acc.nodes += nb;
+    const unsigned long long scanned = warp_sum((unsigned long long)seen);
+    if (lane == 0) {
+        s_acc[warp_in_block()].words += scanned + nb;
+        s_acc[warp_in_block()].nodes += nb;
+    }
     return __ballot_sync(kFull, active && !covered);
 }
 
@@ -1906,14 +1929,19 @@ __device__ __noinline__ void try_donate(const EngineArgs& a, Frame* frames, int 
     __syncwarp();
 }
 
-__device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph, const ResultAcc acc) {
+// Adds the warp's accumulated counts to graph's result and clears them.
+__device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph) {
+    __syncwarp();
     if (lane_id() == 0) {
+        ResultAcc& acc = s_acc[warp_in_block()];
         ResultAcc* r = &a.results[graph];
         if (acc.count) atomicAdd(&r->count, acc.count);
         if (acc.hash) atomicAdd(&r->hash, acc.hash);
         if (acc.nodes) atomicAdd(&r->nodes, acc.nodes);
         if (acc.words) atomicAdd(&r->words, acc.words);
+        acc = ResultAcc{};
     }
+    __syncwarp();
 }
 
 // Children (lanes in `kids`) of a small-record node (L, Q, P) that no row of
@@ -1952,10 +1980,10 @@ __device__ __forceinline__ uint32_t solve_maximal(uint32_t row, uint32_t col, ui
 // frame mirrors level 0 (next = one past the child in progress), so a donor
 // may split the remaining level-0 children off as an ordinary task; the
 // search then drops those it no longer owns.  Warp-collective.
-__device__ __noinline__ ResultAcc solve_small(const EngineArgs& a, const GraphView& G, const uint32_t* nd,
-                                              Frame* frames, int fdepth, bool donate) {
+__device__ __noinline__ void solve_small(const EngineArgs& a, const GraphView& G, const uint32_t* nd, Frame* frames,
+                                         int fdepth, bool donate) {
     const unsigned lane = lane_id();
-    ResultAcc acc{};  // in registers; the caller adds it
+    ResultAcc acc{};  // in registers; committed to the warp's accumulator at the end
     const NodeHdr* h = (const NodeHdr*)nd;
     const RecView R = rec_view(nd);
     const uint32_t n = R.n, nq = R.nq;
@@ -2054,8 +2082,8 @@ __device__ __noinline__ ResultAcc solve_small(const EngineArgs& a, const GraphVi
         }
     }
     if (lane == 0) frames[fdepth].next = frames[fdepth].end;
+    acc_commit(acc);
     __syncwarp();
-    return acc;
 }
 
 #ifdef MBE_PROFILE
@@ -2117,7 +2145,8 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
 #endif
     const bool donate = a.variant != MBE_NOWS;
     const bool prefilter = a.variant != MBE_NOES;
-    ResultAcc acc{};
+    if (lane == 0) s_acc[warp] = ResultAcc{};
+    __syncwarp();
     uint32_t evals = 0, evals_reported = 0;
     for (;;) {
         Popped t;
@@ -2165,7 +2194,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
 #ifdef MBE_PROFILE
             long long c0r = clock64();
 #endif
-            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, arena_top, acc, true, false);
+            ChildOut co = eval_child(a, G, (const uint32_t*)frames[j].node, idx, arena_top, true, false);
 #ifdef MBE_PROFILE
             PROF_TAB(8, c0r, clock64() - c0r);
 #endif
@@ -2225,11 +2254,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
                 const uint32_t* nd = (const uint32_t*)f.node;
                 if (prefilter && (((const NodeHdr*)nd)->flags & kRecPacked) && ((const NodeHdr*)nd)->n <= a.solve_rows) {
                     PROF_T0();
-                    const ResultAcc sa = solve_small(a, G, nd, frames, depth, donate);
-                    acc.count += sa.count;
-                    acc.hash += sa.hash;
-                    acc.nodes += sa.nodes;
-                    acc.words += sa.words;
+                    solve_small(a, G, nd, frames, depth, donate);
                     PROF_ADD(wc.prof, kProfSolve);
                     continue;
                 }
@@ -2240,7 +2265,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
 #ifdef MBE_PROFILE
                     long long c0p = clock64();
 #endif
-                    uint32_t mask = prefilter_w1(R, f.next, nb, acc);
+                    uint32_t mask = prefilter_w1(R, f.next, nb);
 #ifdef MBE_PROFILE
                     PROF_TAB(9, c0p, clock64() - c0p);
             if ((R.flags & kRecPacked) && R.n <= 32) PROF_VAL(wc.prof, kProfSmallPre, clock64() - c0p);
@@ -2271,7 +2296,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
             long long c0e = clock64();
             const uint32_t pW = ((const NodeHdr*)f.node)->W;
 #endif
-            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, arena_top, acc, false, known_max);
+            ChildOut co = eval_child(a, G, (const uint32_t*)f.node, child, arena_top, false, known_max);
 #ifdef MBE_PROFILE
             PROF_TAB(min(7, 31 - __clz(pW)), c0e, clock64() - c0e);
             if ((((const NodeHdr*)f.node)->flags & kRecPacked) && ((const NodeHdr*)f.node)->n <= 32)
@@ -2307,8 +2332,7 @@ __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(cons
             }
             if ((evals & 7u) == 0 && ld_volatile(a.error)) break;
         }
-        flush_acc(a, graph, acc);
-        acc = ResultAcc{};
+        flush_acc(a, graph);
         if (lane == 0) {
             __threadfence();
             atomicSub(a.pending, 1);
