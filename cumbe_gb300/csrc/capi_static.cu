@@ -220,6 +220,7 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     a.a_keys = a_keys;
     a.maxNR = nR;
     a.keys_cap = keys_cap;
+    a.stage_words = 4096;  // the root expansion's L0 staging buffer (dynamic shared memory)
     a.max_n = &ctrl->max_n;
     a.arena = arena;
     a.arena_words = kArenaWords;

@@ -364,12 +364,12 @@ __device__ void root_rlist(uint32_t x, const uint32_t* cl, const uint32_t* cntA,
 // ---------------------------------------------------------------------------
 // Phase A: root expansion
 
-// L0 (the root's neighbour list) staged in shared memory when its 16-byte
-// rounded span fits: words.
+// L0 (the root's neighbour list) staged in shared memory (dynamic, a.stage_words
+// words per block) when its 16-byte rounded span fits.
 constexpr uint32_t kStageWords = 4096;
 
 __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_constant__ EngineArgs a) {
-    __shared__ alignas(16) uint32_t s_L0[kStageWords];
+    extern __shared__ __align__(16) uint32_t s_L0[];
     __shared__ unsigned long long s_bar;
     __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax, s_counted;
     __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
             const uintptr_t beg = (uintptr_t)L0 & ~(uintptr_t)15;
             const uintptr_t end = ((uintptr_t)(L0 + d) + 15) & ~(uintptr_t)15;
             const uintptr_t lim = (uintptr_t)(G.r_adj + G.r_ptr[G.nR] + G.r_adj_slack);
-            if (end - beg <= sizeof(s_L0) && beg >= (uintptr_t)G.r_adj && end <= lim) {
+            if (end - beg <= sizeof(uint32_t) * a.stage_words && beg >= (uintptr_t)G.r_adj && end <= lim) {
                 if (threadIdx.x == 0) bulk_load(s_L0, (const void*)beg, (uint32_t)(end - beg), &s_bar);
                 bool ok = mbar_wait(&s_bar, stage_parity, 1000000000ull);
                 if (!ok) {
@@ -2479,7 +2479,9 @@ static cudaError_t device_facts(int dev, int* n_sm, int* occA, int* occB) {
     if (dev < 0 || dev >= kMaxDev || !known[dev]) {
         int f[3] = {0, 0, 0};
         cudaError_t e = cudaDeviceGetAttribute(&f[0], cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[1], expand_roots_kernel, kThreadsA, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[1], expand_roots_kernel, kThreadsA,
+                                                              sizeof(uint32_t) * kStageWords);
         if (e == cudaSuccess) e = try_dfs_carveout();
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[2], dfs_kernel, kThreadsB, 0);
         if (e != cudaSuccess) return e;
@@ -2687,6 +2689,11 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.error = &ctrl->error;
     a.error_info = &ctrl->error_info;
     a.timeout_ns = cfg.timeout_ns;
+    // L0 staging buffer of the root expansion: none on capped (server)
+    // contexts, whose kernels share SMs with other slots' persistent DFS
+    // blocks -- with 16 KB more shared memory an expansion block no longer
+    // fits beside them and would wait for them to finish.
+    a.stage_words = cfg.mem_cap ? 0u : kStageWords;
     if (cfg.emit) {
         a.emit = 1;
         a.emit_ids = cfg.emit->ids;
@@ -2832,7 +2839,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             eb.ready_clean = 0;
             eb.cmap_clean = 0;
             MBE_CUDA_TRY(cudaEventRecord(e0, s));
-            expand_roots_kernel<<<gridA, kThreadsA, 0, s>>>(a);
+            expand_roots_kernel<<<gridA, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
             MBE_CUDA_TRY(cudaGetLastError());
             MBE_CUDA_TRY(cudaEventRecord(e1, s));
             // DFS scratch is laid out for the largest record this chunk made:
@@ -3011,7 +3018,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 // Launchers for callers outside this file that lay out EngineArgs
 // themselves (the static-scratch entry point in capi_static.cu).
 cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s) {
-    expand_roots_kernel<<<grid, kThreadsA, 0, s>>>(a);
+    expand_roots_kernel<<<grid, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -199,6 +199,7 @@ struct EngineArgs {
     unsigned long long* a_keys;// [gridA][pow2(maxNR)]
     uint32_t maxNR;
     uint32_t keys_cap;
+    uint32_t stage_words;      // dynamic shared words per root-expansion block for staging L0 (0 = none)
     uint32_t* max_n;           // largest candidate count of any root record
     // phase B per-warp memory
     uint32_t* arena;
