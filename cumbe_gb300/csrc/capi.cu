@@ -51,13 +51,12 @@ mbe_status ensure_resident(mbe_ctx* ctx, const mbe_graph* g, const DeviceGraph**
     return MBE_OK;
 }
 
-EngineConfig make_config(mbe_variant v, const mbe_opts* o, bool swapped) {
+EngineConfig make_config(mbe_variant v, const mbe_opts* o) {
     EngineConfig c;
     c.variant = (uint32_t)v;
     if (o) {
-        // thresholds are given in file orientation (rows/cols)
-        c.minL = swapped ? o->min_rows : o->min_cols;
-        c.minR = swapped ? o->min_cols : o->min_rows;
+        c.min_rows = o->min_rows;  // file orientation; each entry maps them to its own
+        c.min_cols = o->min_cols;
         if (o->donate_min) c.donate_min = o->donate_min;
         if (o->blocks_per_sm) c.blocks_per_sm = o->blocks_per_sm;
         if (o->stack_words) c.arena_words = (o->stack_words + 3u) & ~3u;
@@ -149,10 +148,9 @@ namespace mbe {
 // once per orientation group.
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
                     mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
-                    const EmitTarget* emit, uint64_t mem_cap, const BatchKnobs* knobs) {
+                    const EmitTarget* emit, uint64_t mem_cap, const BatchKnobs* knobs,
+                    const std::vector<uint2>* entry_thr) {
     const uint32_t n = (uint32_t)devs.size();
-    bool any_swapped = false, any_plain = false;
-    for (const DeviceGraph* d : devs) (d->swapped ? any_swapped : any_plain) = true;
     std::vector<uint2> roots;
     size_t total = 0;
     for (uint32_t i = 0; i < n; i++) total += devs[i]->nR - devs[i]->n_isolated;
@@ -172,48 +170,22 @@ mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std
         });
     acc.assign(n, ResultAcc{});
     stats = EngineStats{};
-    const bool thresholds = opts && (opts->min_rows || opts->min_cols);
-    const bool split = thresholds && any_swapped && any_plain;
-    for (int pass = 0; pass < 2; pass++) {
-        bool sw = pass == 1;
-        if (sw ? !any_swapped : !any_plain) continue;
-        std::vector<uint2> sel;
-        if (split)
-            for (const uint2& r : roots)
-                if ((bool)devs[r.x]->swapped == sw) sel.push_back(r);
-        EngineConfig cfg = make_config(variant, opts, sw);
-        cfg.emit = emit;
-        cfg.mem_cap = mem_cap;
-        // Many graphs: chunks of ~128 MiB of root records, so that the DFS
-        // reads each chunk's records while they are still in L2 (measured:
-        // 4,096 mixed graphs 19.4 s -> 17.2 s).  One graph keeps one chunk:
-        // every chunk ends in a load-imbalance tail, which costs more there.
-        if (n > 1 && !cfg.pool_words) cfg.chunk_words = 32ull << 20;
-        if (knobs) {
-            if (knobs->blocks_per_sm) cfg.blocks_per_sm = knobs->blocks_per_sm;
-            if (knobs->donate_min) cfg.donate_min = knobs->donate_min;
-            cfg.solve_rows = knobs->solve_rows;
-            if (knobs->chunk_words && !cfg.pool_words) cfg.chunk_words = knobs->chunk_words;
-        }
-        std::vector<ResultAcc> part;
-        EngineStats ps;
-        mbe_status st = engine_run(eb, s, cfg, devs, split ? sel : roots, part, &ps, io);
-        if (st != MBE_OK) return st;
-        for (uint32_t i = 0; i < n; i++) {
-            acc[i].count += part[i].count;
-            acc[i].hash += part[i].hash;
-            acc[i].nodes += part[i].nodes;
-            acc[i].words += part[i].words;
-            acc[i].words_expand += part[i].words_expand;
-        }
-        stats.ms_expand += ps.ms_expand;
-        stats.ms_dfs += ps.ms_dfs;
-        stats.chunks += ps.chunks;
-        stats.grid_a = ps.grid_a;
-        stats.grid_b = ps.grid_b;
-        if (!split) break;
+    EngineConfig cfg = make_config(variant, opts);
+    cfg.emit = emit;
+    cfg.mem_cap = mem_cap;
+    cfg.entry_thr = entry_thr;
+    // Many graphs: chunks of ~128 MiB of root records, so that the DFS
+    // reads each chunk's records while they are still in L2 (measured:
+    // 4,096 mixed graphs 19.4 s -> 17.2 s).  One graph keeps one chunk:
+    // every chunk ends in a load-imbalance tail, which costs more there.
+    if (n > 1 && !cfg.pool_words) cfg.chunk_words = 32ull << 20;
+    if (knobs) {
+        if (knobs->blocks_per_sm) cfg.blocks_per_sm = knobs->blocks_per_sm;
+        if (knobs->donate_min) cfg.donate_min = knobs->donate_min;
+        cfg.solve_rows = knobs->solve_rows;
+        if (knobs->chunk_words && !cfg.pool_words) cfg.chunk_words = knobs->chunk_words;
     }
-    return MBE_OK;
+    return engine_run(eb, s, cfg, devs, roots, acc, &stats, io);
 }
 
 }  // namespace mbe

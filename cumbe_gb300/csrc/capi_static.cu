@@ -190,8 +190,6 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     a.graphs = gview;
     a.n_graphs = 1;
     a.variant = (uint32_t)variant;
-    a.minL = 0;
-    a.minR = 0;
     a.donate_min = 2;
     a.donate_copy = 1;
     a.solve_rows = 32;

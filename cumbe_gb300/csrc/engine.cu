@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
         const GraphView G = a.graphs[rt.x];
         const uint32_t x = rt.y;
         const uint32_t d = G.r_ptr[x + 1] - G.r_ptr[x];
-        if (d == 0 || d < a.minL) continue;  // uniform across the block
+        if (d == 0 || d < G.minL) continue;  // uniform across the block
         const uint32_t* L0 = G.r_adj + G.r_ptr[x];
         const uint32_t W = (d + 31) / 32;
         {
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
         __syncthreads();
         const uint32_t nRset = 1 + s_nabs;
         const uint32_t n2 = s_nq + s_np;
-        const bool emit_task = !s_nonmax && s_np > 0 && nRset + s_np >= a.minR;
+        const bool emit_task = !s_nonmax && s_np > 0 && nRset + s_np >= G.minR;
         const uint64_t rw = a.emit ? record_words_r(W, n2, false, nRset) : record_words(W, n2);
         if (threadIdx.x == 0) {
             s_rec = ~0ull;
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                 unsigned long long words = s_scan * 2 + d;
                 atomicAdd(&r->nodes, 1ull);
                 atomicAdd(&r->words_expand, words);
-                if (!s_nonmax && nRset >= a.minR) {
+                if (!s_nonmax && nRset >= G.minR) {
                     unsigned long long sR = G.eR[x] + s_sabs;
                     atomicAdd(&r->count, 1ull);
                     atomicAdd(&r->hash, (unsigned long long)side_hash(G, s_sl, d, sR, nRset));
@@ -1685,7 +1685,7 @@ ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t
     const unsigned long long sR2 = h->sR + G.eR[cand[xi]] + sabs;
 
     // 4. count + canonical hash
-    if (li >= a.minL && nR2 >= a.minR) {
+    if (li >= G.minL && nR2 >= G.minR) {
         unsigned long long sl = 0;
         if (packed) {
             if ((Li[0] >> lane) & 1u) sl = G.eL[R.map[lane]];  // packed maps hold L vertices
@@ -1708,7 +1708,7 @@ ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t
 
     // 5. child record
     PROF_ADD(wc.prof, kProfExpand);
-    if (npp == 0 || li < a.minL || nR2 + npp < a.minR) return out;
+    if (npp == 0 || li < G.minL || nR2 + npp < G.minR) return out;
     if (packed_child) {
         out = build_packed(a, R, h, xi, li, nnz, Li, Nz, npp, nR2, sR2, keysP, G, arena_top, acc);
         PROF_ADD(wc.prof, kProfBuild);
@@ -2044,13 +2044,13 @@ __device__ __forceinline__ void solve_small(const EngineArgs& a, const GraphView
         const uint32_t nR2 = nR + 1 + __popc(absorbed);
         unsigned long long sR2 = sR + __shfl_sync(kFull, eR, x);
         if (absorbed) sR2 += warp_sum(((absorbed >> lane) & 1u) ? eR : 0ull);
-        if (l2 >= a.minL && nR2 >= a.minR) {
+        if (l2 >= G.minL && nR2 >= G.minR) {
             const unsigned long long sl = warp_sum(((L2 >> lane) & 1u) ? eL : 0ull);
             acc.count++;
             acc.hash += side_hash(G, sl, l2, sR2, nR2);
             if (a.emit) emit_solved(a, G, nd, Rm | (1u << x) | absorbed, L2);
         }
-        if (P2 && l2 >= a.minL && nR2 + __popc(P2) >= a.minR) {
+        if (P2 && l2 >= G.minL && nR2 + __popc(P2) >= G.minR) {
             const uint32_t pend2 = solve_maximal(row, col, L2, Q2, P2, P2);
             acc.nodes += __popc(P2);
             if (pend2) {
@@ -2379,7 +2379,30 @@ void EngineBuffers::release() {
             cudaEventDestroy(e);
             e = nullptr;
         }
+    pin_in.free();
+    pin_out.free();
+    pin_retry.free();
     cmap_clean = ready_clean = 0;
+}
+
+mbe_status HostBuf::ensure(size_t need) {
+    if (need <= bytes) return MBE_OK;
+    free();
+    const size_t want = std::max<size_t>(need, 4096);
+    if (cudaMallocHost(&ptr, want) != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        cudaGetLastError();
+        return fail(MBE_ERR_OUT_OF_MEMORY, "pinned host allocation of " + std::to_string(want) + " bytes failed");
+    }
+    bytes = want;
+    return MBE_OK;
+}
+
+void HostBuf::free() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
 }
 
 mbe_status DevBuf::ensure(size_t need) {
@@ -2626,8 +2649,16 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     }
 
     mbe_status st;
+    // thresholds per entry (the same graph may appear with different ones),
+    // given in file orientation (rows, cols) and stored in L/R orientation
     std::vector<GraphView> views;
-    for (const DeviceGraph* g : gs) views.push_back(view_of(*g));
+    for (uint32_t i = 0; i < ng; i++) {
+        GraphView v = view_of(*gs[i]);
+        const uint2 t = cfg.entry_thr ? (*cfg.entry_thr)[i] : make_uint2(cfg.min_rows, cfg.min_cols);
+        v.minL = gs[i]->swapped ? t.x : t.y;
+        v.minR = gs[i]->swapped ? t.y : t.x;
+        views.push_back(v);
+    }
     if ((st = eb.graphs.ensure(sizeof(GraphView) * ng))) return st;
     if ((st = eb.roots.ensure(sizeof(uint2) * roots.size()))) return st;
     if ((st = eb.ctrl.ensure(sizeof(Ctrl)))) return st;
@@ -2642,8 +2673,19 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * max_frames))) return st;
     if ((st = eb.results.ensure(sizeof(ResultAcc) * ng))) return st;
     if ((st = eb.retry_in.ensure(sizeof(uint32_t) * (size_t)retry_cap))) return st;
-    MBE_CUDA_TRY(cudaMemcpyAsync(eb.graphs.ptr, views.data(), sizeof(GraphView) * ng, cudaMemcpyHostToDevice, s));
-    MBE_CUDA_TRY(cudaMemcpyAsync(eb.roots.ptr, roots.data(), sizeof(uint2) * roots.size(), cudaMemcpyHostToDevice, s));
+    // inputs and readbacks through pinned staging (see HostBuf)
+    const size_t in_views = sizeof(GraphView) * ng, in_roots = sizeof(uint2) * roots.size();
+    const size_t out_res_off = (sizeof(Ctrl) + 15) & ~(size_t)15;
+    const size_t out_retry_off = (out_res_off + sizeof(ResultAcc) * ng + 15) & ~(size_t)15;
+    if ((st = eb.pin_in.ensure(in_views + in_roots))) return st;
+    if ((st = eb.pin_out.ensure(out_retry_off + sizeof(uint32_t) * (size_t)retry_cap))) return st;
+    std::memcpy(eb.pin_in.ptr, views.data(), in_views);
+    std::memcpy((char*)eb.pin_in.ptr + in_views, roots.data(), in_roots);
+    MBE_CUDA_TRY(cudaMemcpyAsync(eb.graphs.ptr, eb.pin_in.ptr, in_views, cudaMemcpyHostToDevice, s));
+    MBE_CUDA_TRY(cudaMemcpyAsync(eb.roots.ptr, (char*)eb.pin_in.ptr + in_views, in_roots, cudaMemcpyHostToDevice, s));
+    Ctrl* const pin_ctrl = (Ctrl*)eb.pin_out.ptr;
+    ResultAcc* const pin_res = (ResultAcc*)((char*)eb.pin_out.ptr + out_res_off);
+    uint32_t* const pin_retry_idx = (uint32_t*)((char*)eb.pin_out.ptr + out_retry_off);
     io->h2d += sizeof(GraphView) * ng + sizeof(uint2) * roots.size();
 
     Ctrl* ctrl = (Ctrl*)eb.ctrl.ptr;
@@ -2652,9 +2694,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.graphs = (const GraphView*)eb.graphs.ptr;
     a.n_graphs = ng;
     a.variant = cfg.variant;
-    a.minL = cfg.minL;
-    a.minR = cfg.minR;
-    a.donate_min = std::max(2u, cfg.donate_min);
+        a.donate_min = std::max(2u, cfg.donate_min);
     a.donate_copy = 1;
     a.solve_rows = std::min<uint32_t>(cfg.solve_rows, kSolveRows);
     if (const char* e = std::getenv("MBE_SOLVE_ROWS")) a.solve_rows = std::min<uint32_t>((uint32_t)std::atoi(e), kSolveRows);
@@ -2818,7 +2858,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 chunk_list = pending_roots;
                 list_n = (uint32_t)chunk_list.size();
                 if ((st = eb.retry_list.ensure(sizeof(uint2) * list_n))) return st;
-                MBE_CUDA_TRY(cudaMemcpyAsync(eb.retry_list.ptr, chunk_list.data(), sizeof(uint2) * list_n,
+                if ((st = eb.pin_retry.ensure(sizeof(uint2) * list_n))) return st;
+                std::memcpy(eb.pin_retry.ptr, chunk_list.data(), sizeof(uint2) * list_n);
+                MBE_CUDA_TRY(cudaMemcpyAsync(eb.retry_list.ptr, eb.pin_retry.ptr, sizeof(uint2) * list_n,
                                              cudaMemcpyHostToDevice, s));
                 io->h2d += sizeof(uint2) * list_n;
                 list = (const uint2*)eb.retry_list.ptr;
@@ -2846,9 +2888,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             // by the kernel itself when the scratch is sized for the bound,
             // else from a readback of that size
             if (!a.scratch_dyn) {
-                uint32_t max_n = 0;
-                MBE_CUDA_TRY(cudaMemcpyAsync(&max_n, &ctrl->max_n, sizeof max_n, cudaMemcpyDeviceToHost, s));
+                MBE_CUDA_TRY(cudaMemcpyAsync(&pin_ctrl->max_n, &ctrl->max_n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
                 MBE_CUDA_TRY(cudaStreamSynchronize(s));
+                const uint32_t max_n = pin_ctrl->max_n;
                 io->d2h += sizeof max_n;
                 uint32_t scr_n = std::max<uint32_t>(max_n, 32);
                 size_t kc = 32;
@@ -2864,14 +2906,14 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             MBE_CUDA_TRY(cudaGetLastError());
             MBE_CUDA_TRY(cudaEventRecord(e2, s));
             io->launches += 2;
-            Ctrl hc;
-            MBE_CUDA_TRY(cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            MBE_CUDA_TRY(cudaMemcpyAsync(pin_ctrl, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
             if (results_with_ctrl) {  // small result sets ride along: one synchronisation per chunk
-                MBE_CUDA_TRY(cudaMemcpyAsync(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng,
-                                             cudaMemcpyDeviceToHost, s));
+                MBE_CUDA_TRY(cudaMemcpyAsync(pin_res, eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost, s));
                 io->d2h += sizeof(ResultAcc) * ng;
             }
             MBE_CUDA_TRY(cudaStreamSynchronize(s));
+            const Ctrl hc = *pin_ctrl;
+            if (results_with_ctrl) std::memcpy(results.data(), pin_res, sizeof(ResultAcc) * ng);
             io->d2h += sizeof(Ctrl);
             float t1 = 0, t2 = 0;
             cudaEventElapsedTime(&t1, e0, e1);
@@ -2901,8 +2943,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             uint32_t consumed = std::min(hc.root_next, list_n);
             std::vector<uint32_t> retry_idx(std::min(hc.n_retry, retry_cap));
             if (!retry_idx.empty()) {
-                MBE_CUDA_TRY(cudaMemcpy(retry_idx.data(), a.retry, sizeof(uint32_t) * retry_idx.size(),
-                                        cudaMemcpyDeviceToHost));
+                MBE_CUDA_TRY(cudaMemcpyAsync(pin_retry_idx, a.retry, sizeof(uint32_t) * retry_idx.size(),
+                                             cudaMemcpyDeviceToHost, s));
+                MBE_CUDA_TRY(cudaStreamSynchronize(s));
+                std::memcpy(retry_idx.data(), pin_retry_idx, sizeof(uint32_t) * retry_idx.size());
                 io->d2h += sizeof(uint32_t) * retry_idx.size();
             }
             if (hc.n_retry > retry_cap || consumed == 0 || consumed == (uint32_t)retry_idx.size()) {
@@ -2938,7 +2982,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         return result;
     }
     if (!results_with_ctrl) {
-        MBE_CUDA_TRY(cudaMemcpy(results.data(), eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost));
+        MBE_CUDA_TRY(cudaMemcpyAsync(pin_res, eb.results.ptr, sizeof(ResultAcc) * ng, cudaMemcpyDeviceToHost, s));
+        MBE_CUDA_TRY(cudaStreamSynchronize(s));
+        std::memcpy(results.data(), pin_res, sizeof(ResultAcc) * ng);
         io->d2h += sizeof(ResultAcc) * ng;
     }
 #ifdef MBE_PROFILE

@@ -166,7 +166,6 @@ struct EngineArgs {
     const GraphView* graphs;
     uint32_t n_graphs;
     uint32_t variant;
-    uint32_t minL, minR;       // thresholds in L/R orientation (batched: same for all)
     uint32_t donate_min;
     uint32_t donate_copy;      // 1: donate small arena records by copy into the pool
     uint32_t solve_rows;       // packed records with at most this many rows (<= 32) are solved in registers

@@ -17,11 +17,23 @@ struct DevBuf {
     void free();
 };
 
+// Pinned host memory reused across calls: every per-launch transfer goes
+// through it, so a copy never takes the driver's pageable path (which
+// returns only when the copy is done and can hold up other streams' small
+// copies while a long kernel runs ahead of it).
+struct HostBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    mbe_status ensure(size_t need);
+    void free();
+};
+
 // Device memory reused across calls on one context.
 struct EngineBuffers {
     DevBuf graphs, roots, ctrl, tasks, ready, cmap, a_cl, a_cnt, a_keys, pool, arena, frames, scratch, results,
         retry_in, retry_list;
     DevBuf e_ids, e_start, e_nrows, e_ncols, e_ctl;  // output stream
+    HostBuf pin_in, pin_out, pin_retry;               // staging of the launch inputs, the readbacks, retry lists
     // sizes chosen at first use from the device's free memory
     uint32_t arena_words = 0;
     uint64_t pool_words = 0;
@@ -50,7 +62,8 @@ struct EmitTarget {
 
 struct EngineConfig {
     uint32_t variant = 0;
-    uint32_t minL = 0, minR = 0;        // thresholds in L/R orientation
+    uint32_t min_rows = 0, min_cols = 0;  // thresholds in file orientation, for every entry ...
+    const std::vector<uint2>* entry_thr = nullptr;  // ... or per entry: (min_rows, min_cols)
     uint32_t donate_min = 2;
     uint32_t blocks_per_sm = 0;         // 0 = occupancy limit
     uint32_t max_frames = 512;
@@ -90,7 +103,8 @@ struct BatchKnobs {
 
 mbe_status run_devs(EngineBuffers& eb, cudaStream_t s, IoCounters* io, const std::vector<const DeviceGraph*>& devs,
                     mbe_variant variant, const mbe_opts* opts, std::vector<ResultAcc>& acc, EngineStats& stats,
-                    const EmitTarget* emit = nullptr, uint64_t mem_cap = 0, const BatchKnobs* knobs = nullptr);
+                    const EmitTarget* emit = nullptr, uint64_t mem_cap = 0, const BatchKnobs* knobs = nullptr,
+                    const std::vector<uint2>* entry_thr = nullptr);
 
 // Resident DFS blocks per SM on device dev (the launch's upper bound).
 cudaError_t dfs_blocks_per_sm(int dev, int* occ);

@@ -47,10 +47,11 @@ struct GraphView {
     const uint32_t* r_orig;
     const uint64_t* eR;
     const uint64_t* eL;
+    uint32_t minL, minR;        // thresholds of this entry, L/R orientation (|L| >= minL, |R| >= minR)
 };
 
 inline GraphView view_of(const DeviceGraph& d) {
-    return GraphView{d.nR, d.nL, d.swapped, kAdjSlack, d.r_ptr, d.r_adj, d.l_ptr, d.l_adj, d.r_orig, d.eR, d.eL};
+    return GraphView{d.nR, d.nL, d.swapped, kAdjSlack, d.r_ptr, d.r_adj, d.l_ptr, d.l_adj, d.r_orig, d.eR, d.eL, 0u, 0u};
 }
 
 mbe_status build_device_graph(const mbe_graph* g, cudaStream_t s, int n_sm, DeviceGraph* out, IoCounters* io);

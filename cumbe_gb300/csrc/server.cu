@@ -5,9 +5,9 @@
 // runs the root-expansion and DFS kernels on `blocks_per_sm` blocks per SM,
 // so launches of different slots share the GPU at the same time.  A slot
 // that becomes free takes, under the queue lock, the oldest waiting request
-// and every later waiting request with the same thresholds (the engine
-// applies one threshold pair per launch) up to max_batch, while the
-// estimated search memory of the batch fits the slot's node-pool share;
+// and later waiting requests (each keeps its own thresholds: the engine
+// applies them per entry, so one launch mixes them) up to max_batch, while
+// the estimated search memory of the batch fits the slot's node-pool share;
 // requests arriving while others run join the next batch of the next free
 // slot.  Heavy requests (estimated search memory above heavy_bytes) are
 // taken by slot 0 only and run alone, so the other slots always serve the
@@ -171,9 +171,9 @@ struct mbe_server {
                     const Req r0 = *first;
                     const bool r0_heavy = r0.est > heavy;
                     uint64_t admitted = 0;
+                    // thresholds travel per request, so one launch mixes them
                     for (auto it = first; it != queue.end() && batch.size() < cfg.max_batch;) {
-                        bool same = it->min_rows == r0.min_rows && it->min_cols == r0.min_cols &&
-                                    (it->est > heavy) == r0_heavy && (batch.empty() || !r0_heavy);
+                        bool same = (it->est > heavy) == r0_heavy && (batch.empty() || !r0_heavy);
                         bool fits = batch.empty() || admitted + it->est <= batch_bytes;
                         if (same && fits) {
                             admitted += it->est;
@@ -202,13 +202,13 @@ struct mbe_server {
             }
             mbe_opts opts;
             std::memset(&opts, 0, sizeof opts);
-            opts.min_rows = batch[0].min_rows;
-            opts.min_cols = batch[0].min_cols;
             opts.blocks_per_sm = cfg.blocks_per_sm;
+            std::vector<uint2> thr;
+            for (const Req& r : batch) thr.push_back(make_uint2(r.min_rows, r.min_cols));
             std::vector<ResultAcc> acc;
             EngineStats stats;
             mbe_status st = run_devs(eb, stream, &io, devs, (mbe_variant)cfg.variant, &opts, acc, stats, nullptr,
-                                     slot_cap);
+                                     slot_cap, nullptr, &thr);
             double t_done = now();
             std::lock_guard<std::mutex> lk(mu);
             slot_bytes[slot] = eb.bytes();

@@ -313,8 +313,9 @@ MBE_API mbe_variant mbe_variant_from_name(const char* name);
  * threads each own a stream and engine buffers and run on a share of the
  * GPU (`blocks_per_sm` DFS blocks per SM), so batches of different slots
  * overlap on the device.  A free slot takes the oldest waiting request
- * plus every later waiting request with the same thresholds, up to
- * `max_batch`, while the estimated root-record memory of the batch fits
+ * plus later waiting requests (whatever their thresholds: one launch applies
+ * each request's own), up to `max_batch`, while the estimated root-record
+ * memory of the batch fits
  * half the slot's share of `mem_budget` (a larger request runs alone).
  * `mem_budget` bounds the device memory of the search: it is divided among
  * the slots up front, and a slot's buffers never outgrow its share (its

@@ -92,3 +92,29 @@ def test_l2_persisting_window_gives_the_same_result(engine):
     for pin in (True, False, True):
         got = engine.enumerate(g, l2_pin=pin)
         assert (got.count, got.hash) == (want.count, want.hash), pin
+
+
+def test_one_batch_with_different_thresholds_per_entry(engine):
+    """Thresholds travel per entry of a launch (the server batches requests
+    with different thresholds together): the same graph twice, and graphs of
+    both orientations, each with its own |A| >= a, |B| >= b, in one batched
+    launch, against the oracle."""
+    import ctypes
+    rng = np.random.default_rng(3)
+    gs = [cm.Graph.from_csr(*random_csr(rng, 40, 70, 0.12)), cm.Graph.from_csr(*random_csr(rng, 80, 35, 0.15))]
+    entries = [(gs[0], 0, 0), (gs[0], 2, 3), (gs[1], 3, 2), (gs[1], 0, 0), (gs[0], 4, 1)]
+    blocker = cm.Graph.generate(2000, 1000, 10000, 2.1, 2.1, 0, 1)  # keeps the slot busy while the rest queue
+    srv = cm.Server(0, slots=1, max_batch=64)
+    try:
+        gids = [srv.add_graph(g) for g in gs]
+        srv.submit(srv.add_graph(blocker))
+        rids = [srv.submit(gids[gs.index(g)], a, b) for g, a, b in entries]
+        out, t0 = [], __import__("time").time()
+        while len(out) < len(rids) + 1 and __import__("time").time() - t0 < 60:
+            out += srv.poll()
+    finally:
+        srv.stop()
+    res = {r["request"]: r for r in out}
+    for rid, (g, a, b) in zip(rids, entries):
+        want = oracle.ref_enumerate(*g.csr(), threads=2, min_rows=a, min_cols=b)
+        assert (res[rid]["count"], res[rid]["hash"]) == (want.count, want.hash), (a, b)
