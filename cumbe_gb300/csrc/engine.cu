@@ -368,6 +368,13 @@ __device__ void root_rlist(uint32_t x, const uint32_t* cl, const uint32_t* cntA,
 // words per block) when its 16-byte rounded span fits.
 constexpr uint32_t kStageWords = 4096;
 
+// kShareSM: the instance capped (server) contexts launch.  Their kernels
+// share SMs with other slots' persistent DFS blocks, so this instance stages
+// nothing and prefers the DFS kernel's shared-memory carveout: a block can
+// then join an SM the other slot's DFS blocks hold (a kernel that prefers
+// another carveout waits for the SM to drain, which kept light requests
+// behind a heavy one for the heavy one's whole run).
+template <bool kShareSM>
 __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_constant__ EngineArgs a) {
     extern __shared__ __align__(16) uint32_t s_L0[];
     __shared__ unsigned long long s_bar;
@@ -426,7 +433,8 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
             const uintptr_t beg = (uintptr_t)L0 & ~(uintptr_t)15;
             const uintptr_t end = ((uintptr_t)(L0 + d) + 15) & ~(uintptr_t)15;
             const uintptr_t lim = (uintptr_t)(G.r_adj + G.r_ptr[G.nR] + G.r_adj_slack);
-            if (end - beg <= sizeof(uint32_t) * a.stage_words && beg >= (uintptr_t)G.r_adj && end <= lim) {
+            if (!kShareSM && end - beg <= sizeof(uint32_t) * a.stage_words && beg >= (uintptr_t)G.r_adj &&
+                end <= lim) {
                 if (threadIdx.x == 0) bulk_load(s_L0, (const void*)beg, (uint32_t)(end - beg), &s_bar);
                 bool ok = mbar_wait(&s_bar, stage_parity, 1000000000ull);
                 if (!ok) {
@@ -2464,7 +2472,8 @@ static cudaError_t set_dfs_carveout() {
             return e;
         int occ = 0;
         if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dfs_kernel, kThreadsB, 0)) != cudaSuccess) return e;
-        if (occ >= MBE_DFS_MIN_BLOCKS) return cudaSuccess;
+        if (occ >= MBE_DFS_MIN_BLOCKS)  // the server's root expansion prefers the same split
+            return cudaFuncSetAttribute(expand_roots_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     }
     return cudaFuncSetAttribute(dfs_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
 }
@@ -2503,7 +2512,7 @@ static cudaError_t device_facts(int dev, int* n_sm, int* occA, int* occB) {
         int f[3] = {0, 0, 0};
         cudaError_t e = cudaDeviceGetAttribute(&f[0], cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[1], expand_roots_kernel, kThreadsA,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[1], expand_roots_kernel<false>, kThreadsA,
                                                               sizeof(uint32_t) * kStageWords);
         if (e == cudaSuccess) e = try_dfs_carveout();
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f[2], dfs_kernel, kThreadsB, 0);
@@ -2881,7 +2890,10 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             eb.ready_clean = 0;
             eb.cmap_clean = 0;
             MBE_CUDA_TRY(cudaEventRecord(e0, s));
-            expand_roots_kernel<<<gridA, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
+            if (cfg.mem_cap)
+                expand_roots_kernel<true><<<gridA, kThreadsA, 0, s>>>(a);
+            else
+                expand_roots_kernel<false><<<gridA, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
             MBE_CUDA_TRY(cudaGetLastError());
             MBE_CUDA_TRY(cudaEventRecord(e1, s));
             // DFS scratch is laid out for the largest record this chunk made:
@@ -3064,7 +3076,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
 // Launchers for callers outside this file that lay out EngineArgs
 // themselves (the static-scratch entry point in capi_static.cu).
 cudaError_t launch_expand_roots(const EngineArgs& a, unsigned grid, cudaStream_t s) {
-    expand_roots_kernel<<<grid, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
+    expand_roots_kernel<false><<<grid, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
     return cudaGetLastError();
 }
 
