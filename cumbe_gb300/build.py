@@ -45,7 +45,7 @@ def _flags() -> list[str]:
     # MBE_DFS_WARPS=N sets its warps per block; default 4.
     if os.environ.get("MBE_DFS_WARPS"):
         f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]
-    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX", "MBE_SMEM_W", "MBE_SH_ROWS"):  # tuning sweeps
+    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX", "MBE_SMEM_W", "MBE_SH_ROWS", "MBE_POLL_CYCLES"):  # sweeps
         if os.environ.get(knob):
             f += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if os.environ.get("MBE_EVAL_NOINLINE") == "1":
