@@ -37,7 +37,7 @@ def _flags() -> list[str]:
     if os.environ.get("MBE_PROFILE") == "1":
         f += ["-DMBE_PROFILE"]
     # MBE_DFS_BLOCKS=N sets the resident blocks per SM the enumeration kernel
-    # is compiled for (its register budget); default 6.
+    # is compiled for (its register budget); default 7.
     if os.environ.get("MBE_DFS_BLOCKS"):
         f += ["-DMBE_DFS_MIN_BLOCKS=%d" % int(os.environ["MBE_DFS_BLOCKS"])]
     # MBE_UNROLL=E,G,P sets the scan unroll factors of the enumeration kernel

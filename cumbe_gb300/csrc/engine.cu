@@ -37,11 +37,13 @@ constexpr int kWarpsB = kDfsWarps;
 constexpr int kThreadsB = kWarpsB * 32;
 // Shared-memory sizes per DFS warp, chosen so that MBE_DFS_MIN_BLOCKS
 // blocks fit the 64 KB carveout (the rest of the SM's memory stays L1).
+// At seven blocks: 16 L_i words and 24 packed-build rows (26/16 measured
+// the same, 30/8 and 16/16 slower).
 #ifndef MBE_SMEM_W
-#define MBE_SMEM_W 32
+#define MBE_SMEM_W 16
 #endif
 #ifndef MBE_SH_ROWS
-#define MBE_SH_ROWS 40
+#define MBE_SH_ROWS 24
 #endif
 constexpr uint32_t kSmemW = MBE_SMEM_W;  // Li words cached in shared memory per warp
 constexpr unsigned long long kInvalidKey = ~0ull;
@@ -1621,9 +1623,11 @@ ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t
     const uint32_t* M0 = M + (size_t)(nnz ? Nz[0] : 0u) * n;
     const uint32_t L0 = Li[0];
 
-    // 2. maximality against Q u P[0..i); counts kept for Q'
+    // 2. maximality against Q u P[0..i); counts kept for Q' of a wide child
+    // (a packed child, |L_i| <= 32, regathers its rows and never reads them)
     if (!known_max) {
         const bool es = a.variant != MBE_NOES;
+        const bool keep_counts = li > 32;
         bool maximal = true;
         for (uint32_t base = 0; base < xi; base += 32) {
             uint32_t c = base + lane;
@@ -1633,7 +1637,7 @@ ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t
                     cc = __popc(M0[c] & L0);
                 else
                     for (uint32_t k = 0; k < nnz; k++) cc += __popc(M[(size_t)Nz[k] * n + c] & Li[k]);
-                wc.scrQcnt[c] = cc;
+                if (keep_counts) wc.scrQcnt[c] = cc;
             }
             unsigned full = __ballot_sync(kFull, c < xi && cc == li);
             acc.words += (unsigned long long)nnz * min(32u, xi - base);
@@ -1956,6 +1960,23 @@ __device__ __noinline__ void flush_acc(const EngineArgs& a, uint32_t graph) {
     __syncwarp();
 }
 
+// 32 x 32 bit transpose across the warp: lane i holds row i on entry, lane
+// b holds column b (bit i = bit b of row i) on return.  Five rounds swap the
+// off-diagonal blocks of width 16, 8, 4, 2 and 1 with the partner lane i ^ s
+// (each round exchanges one bit of the row index with the same bit of the
+// column index); five shuffles instead of 32 ballots.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+    const unsigned lane = lane_id();
+    constexpr uint32_t kMask[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const uint32_t sh = 16u >> k, m = kMask[k];
+        const uint32_t y = __shfl_xor_sync(kFull, x, sh);
+        x = (lane & sh) ? ((x & ~m) | ((y >> sh) & m)) : ((x & m) | ((y & m) << sh));
+    }
+    return x;
+}
+
 // Children (lanes in `kids`) of a small-record node (L, Q, P) that no row of
 // Q, nor an earlier row of P, covers.  One lane per child x: its coverers are
 // the rows holding every bit of L_x = L & row_x, i.e. the AND over those bits
@@ -2004,12 +2025,7 @@ __device__ __forceinline__ void solve_small(const EngineArgs& a, const GraphView
     const uint32_t n = R.n, nq = R.nq;
     const uint32_t row = lane < n ? R.M[lane] : 0u;
     // transpose: lane b holds the rows that contain bit b of the record's L
-    uint32_t col = 0;
-#pragma unroll 4
-    for (uint32_t b = 0; b < 32; b++) {
-        const uint32_t cb = __ballot_sync(kFull, (row >> b) & 1u);
-        if (lane == b) col = cb;
-    }
+    const uint32_t col = warp_transpose32(row);
     const unsigned long long eR = lane < n ? G.eR[R.cand[lane]] : 0ull;
     const uint32_t Lroot = R.Lm[0];
     const unsigned long long eL = ((Lroot >> lane) & 1u) ? G.eL[R.map[lane]] : 0ull;  // packed maps hold L vertices

@@ -26,16 +26,16 @@
 namespace mbe {
 
 // Shape of the DFS kernel: warps per block and the resident blocks per SM
-// it is compiled for (the register budget).  4 x 6 = 24 warps per SM at 80
-// registers measured fastest once the warp-uniform state moved from local
-// to shared memory (bench graph: 5 blocks 254.5 ms, 6 blocks 248.0 ms,
-// 8 blocks 264 ms; with 6 blocks the shared arrays are trimmed so the six
-// fit a 64 KB carveout: 246.3 ms).
+// it is compiled for (the register budget).  4 x 7 = 28 warps per SM at 72
+// registers measured fastest, with the shared arrays trimmed so that seven
+// blocks fit a 64 KB carveout (bench graph: 6 blocks at 80 registers
+// 233.7 ms, 7 blocks 229.0 ms, 8 blocks at 64 registers 239.4 ms; 600-graph
+// batch 2,972 / 2,796 / 2,890 ms).
 #ifndef MBE_DFS_WARPS
 #define MBE_DFS_WARPS 4
 #endif
 #ifndef MBE_DFS_MIN_BLOCKS
-#define MBE_DFS_MIN_BLOCKS 6
+#define MBE_DFS_MIN_BLOCKS 7
 #endif
 constexpr int kDfsWarps = MBE_DFS_WARPS;
 
