@@ -41,7 +41,7 @@ def _flags() -> list[str]:
     if os.environ.get("MBE_DFS_BLOCKS"):
         f += ["-DMBE_DFS_MIN_BLOCKS=%d" % int(os.environ["MBE_DFS_BLOCKS"])]
     # MBE_UNROLL=E,G,P sets the scan unroll factors of the enumeration kernel
-    # (expansion chunks, gather chunks, prefilter rows); default 1,1,6.
+    # (expansion chunks, gather chunks, prefilter rows); default 1,1,5.
     # MBE_DFS_WARPS=N sets its warps per block; default 4.
     if os.environ.get("MBE_DFS_WARPS"):
         f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]

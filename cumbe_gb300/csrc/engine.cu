@@ -62,11 +62,11 @@ constexpr uint32_t kShRows = MBE_SH_ROWS;  // Q' rows / P' keys of a packed buil
 #ifndef MBE_UNROLL_G
 #define MBE_UNROLL_G 1
 #endif
-// Prefilter rows in flight per lane: 6 measured fastest on the bench graph
-// at 7 blocks per SM (2 to 6 within 0.5 ms of each other, 8 2.4% slower; 8
-// was 1.2% faster on the mixed batch).
+// Prefilter rows in flight per lane: 5 measured fastest on the bench graph
+// at 7 blocks per SM (2 to 6 within 1% of each other, 8 2.4% slower; 8 was
+// 1.2% faster on the mixed batch).
 #ifndef MBE_UNROLL_P
-#define MBE_UNROLL_P 6
+#define MBE_UNROLL_P 5
 #endif
 constexpr int kUnrollE = MBE_UNROLL_E;   // 32-row chunks in flight per step of the expansion scan
 constexpr int kUnrollG = MBE_UNROLL_G;   // ... of the Q' gather of a packed build
