@@ -970,7 +970,7 @@ struct RecView {
     const uint32_t* map;   // wmap[W], or lmap[32] when packed
     const uint32_t* Lm;
     const uint32_t* cand;
-    const uint32_t* cnt;
+    const uint32_t* cnt;   // nullptr when packed: a count is the row's popcount
     const uint32_t* M;
 };
 
@@ -984,8 +984,9 @@ __device__ __forceinline__ RecView rec_view(const uint32_t* nd) {
     v.map = nd + kHdrWords;
     v.Lm = v.map + ((v.flags & kRecPacked) ? 32u : pad4(v.W));
     v.cand = v.Lm + pad4(v.W);
-    v.cnt = v.cand + pad4(v.n);
-    v.M = v.cnt + pad4(v.n);
+    const bool packed = (v.flags & kRecPacked) != 0;
+    v.cnt = packed ? nullptr : v.cand + pad4(v.n);
+    v.M = v.cand + (packed ? 1u : 2u) * pad4(v.n);
     return v;
 }
 
@@ -1286,8 +1287,7 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     uint32_t* map2 = rec + kHdrWords;
     uint32_t* Lm2 = map2 + 32;
     uint32_t* cand2 = Lm2 + 4;
-    uint32_t* cnt2 = cand2 + pad4(n2);
-    uint32_t* M2 = cnt2 + pad4(n2);
+    uint32_t* M2 = cand2 + pad4(n2);  // no count array: counts are row popcounts
     if (lane == 0) {
         NodeHdr* h2 = (NodeHdr*)rec;
         h2->graph = h->graph;
@@ -1326,7 +1326,6 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
     }
     for (uint32_t t = lane; t < nq2; t += 32) {
         cand2[t] = R.cand[spos[t]];
-        cnt2[t] = 0;
         M2[t] = nnz == 1 ? compress32(srow[t], plan0) : srow[t];
     }
     for (uint32_t base = 0; base < npp; base += 32) {
@@ -1340,7 +1339,6 @@ __device__ ChildOut build_packed(const EngineArgs& a, const RecView& R, const No
             uint32_t dst = nq2 + off + __popc(grp & lanemask_lt());
             uint32_t c = nq + (uint32_t)key;
             cand2[dst] = R.cand[c];
-            cnt2[dst] = cc;
             M2[dst] = nnz == 1 ? compress32(M0[c], plan0) : packed_row(M, n, Nz, Li, nnz, c, plan0);
         }
         __syncwarp();
@@ -1599,7 +1597,7 @@ ChildOut eval_child_impl(const EngineArgs& a, const GraphView& G, const uint32_t
     const uint32_t* M = R.M;
     const uint32_t* cand = R.cand;
     const uint32_t xi = nq + i;
-    const uint32_t li = R.cnt[xi];
+    const uint32_t li = packed ? __popc(M[xi]) : R.cnt[xi];
     uint32_t* Li = W <= kSmemW ? s_Li[wb] : wc.scrLi;
     uint32_t* Nz = W <= kSmemW ? s_Nz[wb] : wc.scrNz;
     ChildOut out{nullptr, 0, 0, 0ull};
@@ -1775,10 +1773,15 @@ __device__ uint32_t prefilter_w1(const RecView& R, uint32_t base, uint32_t nb) {
     uint32_t plo = lim;
     if (active) {
         const uint32_t li = __popc(Li);
+        // counts: the record's count array, or the row popcounts of a
+        // packed record (which stores none)
+        const bool packed = (R.flags & kRecPacked) != 0;
+        const uint32_t* cs = packed ? R.M : R.cnt;
         uint32_t lo = nq, hi = xi;
         while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
-            if (R.cnt[mid] < li)
+            const uint32_t v = cs[mid];
+            if ((packed ? (uint32_t)__popc(v) : v) < li)
                 lo = mid + 1;
             else
                 hi = mid;

@@ -49,7 +49,8 @@ __host__ __device__ inline uint32_t pad4(uint32_t x) { return (x + 3u) & ~3u; }
 //   wmap[W]     root word index of each word (lmap[32] when packed)
 //   Lm[W]       L as bits per word
 //   cand[n]     candidate ranks; [0,nq) = Q part, [nq,n) = P part
-//   cnt[n]      |N(v) n L| (P part)
+//   cnt[n]      |N(v) n L| (P part); absent when packed, where a row is one
+//               word holding only L's bits and its count is the row's popcount
 //   M[W*n]      word-major bit rows
 struct NodeHdr {
     uint32_t graph;
@@ -105,9 +106,11 @@ enum : int {
 
 // A packed record (|L| <= 32) keeps its L bits dense in one word and maps
 // bit t to root bit lmap[t] (32 words); otherwise word k of a row is root
-// word wmap[k].
+// word wmap[k].  A packed record stores no count array: its counts are the
+// popcounts of its one-word rows.
 __host__ __device__ inline uint64_t record_words(uint32_t W, uint32_t n, bool packed = false) {
-    return kHdrWords + (packed ? 32ull : pad4(W)) + pad4(W) + 2ull * pad4(n) + (((uint64_t)W * n + 3) & ~3ull);
+    return kHdrWords + (packed ? 32ull : pad4(W)) + pad4(W) + (packed ? 1ull : 2ull) * pad4(n) +
+           (((uint64_t)W * n + 3) & ~3ull);
 }
 
 // Words of a record that also carries its R list (nr ranks; output stream
