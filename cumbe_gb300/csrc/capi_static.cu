@@ -221,9 +221,12 @@ extern "C" mbe_status mbe_enumerate_static(uint32_t n_rows, uint32_t n_cols, con
     a.stage_words = 4096;  // the root expansion's L0 staging buffer (dynamic shared memory)
     a.max_n = &ctrl->max_n;
     a.arena = arena;
-    a.arena_words = kArenaWords;
+    a.arena_stride = kArenaWords;
+    a.arena_words = arena_usable_words(kArenaWords);
     a.frames = frames;
     a.max_frames = kMaxFrames;
+    a.frame_stride = kMaxFrames;
+    a.frame_skew = 0;
     a.scratch = scratch;
     a.scratch_words = (uint32_t)sw;
     a.scr_n = scr_n;

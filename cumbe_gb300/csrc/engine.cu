@@ -2141,11 +2141,11 @@ __device__ void prof_idle(const EngineArgs& a, unsigned long long t0, unsigned l
 __global__ void __launch_bounds__(kThreadsB, MBE_DFS_MIN_BLOCKS) dfs_kernel(const __grid_constant__ EngineArgs a) {
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const size_t gw = (size_t)blockIdx.x * kWarpsB + warp;
-    Frame* frames = a.frames + gw * a.max_frames;
+    Frame* frames = a.frames + gw * a.frame_stride + (a.frame_skew ? frame_skew((uint32_t)gw) : 0u);
     WarpCtx& wc = s_wc[warp];
     uint32_t arena_top = 0;  // words of this warp's arena in use (warp-uniform)
     if (lane == 0) {
-        wc.arena = a.arena + gw * a.arena_words;
+        wc.arena = a.arena + gw * a.arena_stride + arena_skew((uint32_t)gw, a.arena_stride);
         // scratch layout (scratch_words): scr_n from the largest root record
         // of the chunk, kc the power of two >= scr_n
         uint32_t scr_n = a.scr_n, kc = a.scr_kc;
@@ -2670,7 +2670,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
             held(eb.a_cnt, sizeof(uint32_t) * (size_t)gridA * maxNR) +
             held(eb.a_keys, sizeof(unsigned long long) * (size_t)gridA * keys_cap) +
             held(eb.arena, sizeof(uint32_t) * (size_t)nwarpsB * arena_words) +
-            held(eb.frames, sizeof(Frame) * (size_t)nwarpsB * max_frames) + held(eb.results, sizeof(ResultAcc) * ng) +
+            held(eb.frames, sizeof(Frame) * (size_t)nwarpsB * (max_frames + kFrameSlack)) + held(eb.results, sizeof(ResultAcc) * ng) +
             held(eb.retry_in, sizeof(uint32_t) * (size_t)retry_cap) +
             held(eb.retry_list, sizeof(uint2) * roots.size()) +
             held(eb.scratch, sizeof(uint32_t) * (size_t)nwarpsB * scratch_words(maxW, scr_b, kc_b, cfg.emit != nullptr));
@@ -2712,7 +2712,7 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     if ((st = eb.a_cnt.ensure(sizeof(uint32_t) * (size_t)gridA * maxNR))) return st;
     if ((st = eb.a_keys.ensure(sizeof(unsigned long long) * (size_t)gridA * keys_cap))) return st;
     if ((st = eb.arena.ensure(sizeof(uint32_t) * (size_t)nwarpsB * arena_words))) return st;
-    if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * max_frames))) return st;
+    if ((st = eb.frames.ensure(sizeof(Frame) * (size_t)nwarpsB * (max_frames + kFrameSlack)))) return st;
     if ((st = eb.results.ensure(sizeof(ResultAcc) * ng))) return st;
     if ((st = eb.retry_in.ensure(sizeof(uint32_t) * (size_t)retry_cap))) return st;
     // inputs and readbacks through pinned staging (see HostBuf)
@@ -2763,9 +2763,12 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     a.keys_cap = keys_cap;
     a.max_n = &ctrl->max_n;
     a.arena = (uint32_t*)eb.arena.ptr;
-    a.arena_words = arena_words;
+    a.arena_stride = arena_words;
+    a.arena_words = arena_usable_words(arena_words);
     a.frames = (Frame*)eb.frames.ptr;
     a.max_frames = max_frames;
+    a.frame_stride = max_frames + kFrameSlack;
+    a.frame_skew = 1;
     a.max_W = maxW;
     a.results = (ResultAcc*)eb.results.ptr;
     a.error = &ctrl->error;

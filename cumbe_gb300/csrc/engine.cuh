@@ -44,6 +44,31 @@ constexpr uint32_t kMaxPath = 27;
 
 __host__ __device__ inline uint32_t pad4(uint32_t x) { return (x + 3u) & ~3u; }
 
+// Per-warp DFS arenas sit at a fixed stride (a multiple of 4 MiB by
+// default), so without an offset every warp's hot stack top would fall on
+// the same cache sets.  Warp gw's arena starts arena_skew(gw, stride) words
+// into its region: one of up to 32 128-byte line offsets, chosen by a
+// multiplicative hash of gw (warps of blocks resident on one SM differ in
+// gw by multiples of the grid's block count).  The slack the largest offset
+// takes is at most a sixteenth of the stride.
+__host__ __device__ inline uint32_t arena_skew_lines(uint32_t stride) {
+    const uint32_t l = stride / 512u;
+    return l < 32u ? l : 32u;
+}
+__host__ __device__ inline uint32_t arena_usable_words(uint32_t stride) {
+    const uint32_t l = arena_skew_lines(stride);
+    return l ? stride - (l - 1u) * 32u : stride;
+}
+__host__ __device__ inline uint32_t arena_skew(uint32_t gw, uint32_t stride) {
+    const uint32_t l = arena_skew_lines(stride);
+    return l ? (((gw * 2654435761u) >> 16) % l) * 32u : 0u;
+}
+// The same for the per-warp frame stacks (512 frames of 32 bytes, a 16 KB
+// stride): one of 32 line offsets (4 frames each), so the region of a warp
+// holds kFrameSlack frames more than its stack.
+constexpr uint32_t kFrameSlack = 31u * 4u;
+__host__ __device__ inline uint32_t frame_skew(uint32_t gw) { return (((gw * 2654435761u) >> 16) % 32u) * 4u; }
+
 // record layout (32-bit words):
 //   [0,16)      header
 //   wmap[W]     root word index of each word (lmap[32] when packed)
@@ -205,9 +230,12 @@ struct EngineArgs {
     uint32_t* max_n;           // largest candidate count of any root record
     // phase B per-warp memory
     uint32_t* arena;
-    uint32_t arena_words;
+    uint32_t arena_words;      // usable words of one warp's arena
+    uint32_t arena_stride;     // words between consecutive warps' arena regions
     Frame* frames;
     uint32_t max_frames;
+    uint32_t frame_stride;     // frames between consecutive warps' stacks (>= max_frames)
+    uint32_t frame_skew;       // 1: stacks start at hashed line offsets (frame_stride >= max_frames + kFrameSlack)
     uint32_t* scratch;
     uint32_t scratch_words;
     uint32_t scr_n;            // candidate bound the scratch is laid out for
