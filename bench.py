@@ -443,10 +443,13 @@ def reference_gpu_leg(eng, workload="power_law_94k_30k_e100k"):
 # as the kernel's word counter defined them when these figures were fixed
 # (1.2040e10 words per launch on the 293,000-edge graph).  The
 # figure is held fixed so that a kernel that skips work shows as a higher
-# achieved rate on the same work, never as a smaller numerator; the live
-# counter of the running build is reported beside it.
+# achieved rate on the same work, never as a smaller numerator.  The
+# counter itself is a diagnostic compiled into MBE_COUNT_WORDS=1 builds
+# only; when the running build has it, its live figure is reported beside
+# the frozen one (null otherwise).
 FROZEN_ALGORITHMIC_BYTES = {
     "power_law_94k_30k": 48_160_205_850,
+    "power_law_94k_30k_e100k": 711_051_424,
 }
 
 
@@ -541,15 +544,17 @@ def main():
     # ---- roofline of the dominant kernel (dfs_kernel) ----
     peak, peak_kind = peak_hbm()
     launch_ms = tot_dfs_ms / args.steps
-    live_bytes = tot_words * 4 // args.steps
+    live_bytes = tot_words * 4 // args.steps if tot_words else None  # None: counter compiled out
     frozen = FROZEN_ALGORITHMIC_BYTES.get(args.workload) if world == 1 else None
     alg_bytes = frozen if frozen is not None else live_bytes
-    achieved = alg_bytes / (launch_ms / 1000.0) / 1e9 if launch_ms > 0 else 0.0
+    achieved = alg_bytes / (launch_ms / 1000.0) / 1e9 if alg_bytes is not None and launch_ms > 0 else None
     traffic = profile_traffic(args.workload)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved is not None else None,
                 "traffic": traffic, "peak_source": peak_kind, "kernel": "dfs_kernel",
                 "algorithmic_bytes_per_launch": alg_bytes,
-                "numerator": "frozen per workload" if frozen is not None else "live kernel word counter",
+                "numerator": "frozen per workload" if frozen is not None else (
+                    "live kernel word counter" if live_bytes is not None else "none (counter compiled out)"),
                 "live_counter_bytes_per_launch": live_bytes,
                 "launch_ms": launch_ms,
                 "dram_bytes_per_launch_ncu": traffic,

@@ -36,6 +36,8 @@ def _flags() -> list[str]:
     # (printed to stderr after each enumeration); off by default.
     if os.environ.get("MBE_PROFILE") == "1":
         f += ["-DMBE_PROFILE"]
+    # MBE_COUNT_WORDS=1 compiles the DFS kernel's set-word counter in
+    # (mbe_result.words); off by default, on in MBE_PROFILE=1 builds.
     # MBE_DFS_BLOCKS=N sets the resident blocks per SM the enumeration kernel
     # is compiled for (its register budget); default 7.
     if os.environ.get("MBE_DFS_BLOCKS"):
@@ -45,7 +47,7 @@ def _flags() -> list[str]:
     # MBE_DFS_WARPS=N sets its warps per block; default 4.
     if os.environ.get("MBE_DFS_WARPS"):
         f += ["-DMBE_DFS_WARPS=%d" % int(os.environ["MBE_DFS_WARPS"])]
-    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX", "MBE_SMEM_W", "MBE_SH_ROWS", "MBE_POLL_CYCLES"):  # sweeps
+    for knob in ("MBE_KEEP_WINDOW", "MBE_POP_SLEEP_MAX", "MBE_SMEM_W", "MBE_SH_ROWS", "MBE_POLL_CYCLES", "MBE_COUNT_WORDS"):  # sweeps
         if os.environ.get(knob):
             f += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if os.environ.get("MBE_EVAL_NOINLINE") == "1":

@@ -167,7 +167,9 @@ typedef struct mbe_result {
     uint64_t hash;               /* sum over bicliques of mbe_biclique_hash */
     uint64_t nodes;              /* search-tree nodes evaluated             */
     uint64_t words;              /* 32-bit words of set data streamed by
-                                    the DFS kernel                          */
+                                    the DFS kernel; a diagnostic counted
+                                    only by builds with MBE_COUNT_WORDS=1
+                                    or MBE_PROFILE=1, else 0               */
     uint64_t words_expand;       /* words streamed by the root expansion    */
     uint64_t emitted;            /* bicliques written to emit buffers       */
     float ms;                    /* device time of the enumeration kernels  */
