@@ -187,10 +187,12 @@ def cpu_baseline(csr, wl, threads, stride_mult=1):
 
 def batched_leg(eng, n_graphs=4096):
     """Batched workload: n_graphs graphs (workloads.batch) through
-    mbe_batch_run with the engine defaults, then autotuned (mbe_batch_tune
-    on the same graphs, its wall time reported apart), vs one launch pair per
-    graph.  Per-graph counts and hashes must agree between all three and
-    with the committed oracle results for the graphs they cover."""
+    mbe_batch_run with the engine defaults (chunks launched as a captured
+    CUDA graph), the same with the host-driven chunk loop, then autotuned
+    (mbe_batch_tune on the same graphs, its wall time reported apart), vs one
+    launch pair per graph.  Per-graph counts and hashes must agree between
+    all four and with the committed oracle results for the graphs they
+    cover."""
     import cumbe_gb300 as cm
     from cumbe_gb300 import workloads
     ps = workloads.batch(n_graphs)
@@ -202,6 +204,9 @@ def batched_leg(eng, n_graphs=4096):
     t0 = time.perf_counter()
     res, ms = eng.batch(gs)
     batched_wall = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    res_h, ms_h = eng.batch(gs, host_chunks=True)
+    host_wall = (time.perf_counter() - t0) * 1e3
     t0 = time.perf_counter()
     choices = eng.batch_tune(gs)
     tune_wall = (time.perf_counter() - t0) * 1e3
@@ -216,6 +221,7 @@ def batched_leg(eng, n_graphs=4096):
         q = eng.enumerate(g)
         plain_ms += q.ms
         mismatches += (q.count, q.hash) != (r.count, r.hash) or (rt.count, rt.hash) != (r.count, r.hash)
+    mismatches += sum((rh.count, rh.hash) != (r.count, r.hash) for r, rh in zip(res, res_h))
     plain_wall = (time.perf_counter() - t0) * 1e3
     fix = json.load(open(os.path.join(ROOT, "tests", "golden", "batch_oracle.json")))["graphs"]
     fixture_checked = fixture_mismatches = 0
@@ -227,13 +233,17 @@ def batched_leg(eng, n_graphs=4096):
     for g in gs:
         eng.release(g)
     return {"graphs": n_graphs, "bicliques": total, "batched_ms": ms, "tuned_ms": ms_t, "plain_ms": plain_ms,
+            "host_chunks_ms": ms_h,
             "batched_wall_ms": batched_wall, "tuned_wall_ms": tuned_wall, "plain_wall_ms": plain_wall,
+            "host_chunks_wall_ms": host_wall,
             "tuning_wall_ms": tune_wall,
             "batched_bicliques_per_s": total / (ms / 1e3), "tuned_bicliques_per_s": total / (ms_t / 1e3),
             "plain_bicliques_per_s": total / (plain_ms / 1e3),
             "tune_choices": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in c.items()} for c in choices],
             "note": "_ms = device time of the enumeration kernels (CUDA events); _wall_ms = host wall clock "
-                    "of the whole call(s), graphs resident; tuning = mbe_batch_tune's sweep, untimed",
+                    "of the whole call(s), graphs resident; batched/tuned: chunks launched as a captured CUDA "
+                    "graph (8 per launch); host_chunks: the host-driven chunk loop; tuning = mbe_batch_tune's "
+                    "sweep, untimed",
             "per_graph_mismatches": mismatches,
             "oracle_fixture": {"graphs_checked": fixture_checked, "mismatches": fixture_mismatches},
             "workload": "4,096 uniform random graphs, |U| log-uniform [50,5000], |V|=|U|/2, "

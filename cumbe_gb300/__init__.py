@@ -28,6 +28,7 @@ OPT_NO_HASH = 1
 OPT_EMIT = 2
 OPT_TIMING = 4
 OPT_L2_PIN = 8
+OPT_HOST_CHUNKS = 16
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "IO", 3: "FORMAT", 4: "CUDA", 5: "OUT_OF_MEMORY",
           6: "DEVICE_TIMEOUT", 7: "CAPACITY", 8: "NO_DEVICE", 9: "BUSY"}
@@ -344,12 +345,16 @@ class Engine:
         return out
 
     def batch(self, graphs: list[Graph], variant: str = "cuMBE", min_rows: int = 0, min_cols: int = 0,
-              **tuning) -> tuple[list[Result], float]:
+              host_chunks: bool = False, **tuning) -> tuple[list[Result], float]:
+        """mbe_batch_run over `graphs`.  Its chunks launch as a captured CUDA
+        graph; host_chunks=True drives them from the host instead
+        (MBE_OPT_HOST_CHUNKS)."""
         n = len(graphs)
         arr = (_VP * n)(*[g.handle for g in graphs])
         res = (_Result * n)()
         tot = ctypes.c_float(0)
-        o = _opts(flags=OPT_TIMING, min_rows=min_rows, min_cols=min_cols, **tuning)
+        o = _opts(flags=OPT_TIMING | (OPT_HOST_CHUNKS if host_chunks else 0), min_rows=min_rows, min_cols=min_cols,
+                  **tuning)
         _check(lib().mbe_batch_run(self._h, arr, n, VARIANTS[variant], ctypes.byref(o), res, ctypes.byref(tot)),
                "mbe_batch_run")
         return [Result(r.count, r.hash, r.nodes, r.words, r.words_expand, r.ms, r.ms_prep) for r in res], tot.value

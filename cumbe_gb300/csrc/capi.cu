@@ -54,6 +54,12 @@ mbe_status ensure_resident(mbe_ctx* ctx, const mbe_graph* g, const DeviceGraph**
 EngineConfig make_config(mbe_variant v, const mbe_opts* o) {
     EngineConfig c;
     c.variant = (uint32_t)v;
+    // multi-graph runs launch their chunks as a captured CUDA graph, 8 chunks
+    // per launch, unless the caller asks for the host-driven loop
+    c.graph_chunks = 8;
+    if (const char* env = std::getenv("MBE_GRAPH_CHUNKS"))
+        c.graph_chunks = (uint32_t)std::max(1ul, std::strtoul(env, nullptr, 10));
+    if (o && (o->flags & MBE_OPT_HOST_CHUNKS)) c.graph_chunks = 0;
     if (o) {
         c.min_rows = o->min_rows;  // file orientation; each entry maps them to its own
         c.min_cols = o->min_cols;

@@ -2503,6 +2503,28 @@ struct Ctrl {
     uint32_t max_n;
     uint32_t pad[2];
 };
+
+// Device-driven chunk loop (graph mode): runs before each chunk's root
+// expansion in the captured sequence and resets what the host resets
+// between chunks -- the node pool and the task ring's counters (the ring's
+// flags and the candidate maps are clean after a chunk that ended without
+// an error).  The root cursor carries over, so each chunk resumes where the
+// previous one stopped; once it is past the last root, the chunk's kernels
+// find nothing to do.  A root whose record did not fit the pool would need
+// the host's re-queueing: it is reported as pool exhaustion, and the host
+// runs the batch again with its own chunk loop.
+__global__ void chunk_prep_kernel(Ctrl* c) {
+    if (threadIdx.x != 0 || c->error) return;
+    if (c->n_retry) {
+        c->error = kErrPool;
+        c->error_info = c->n_retry;
+        return;
+    }
+    c->pool_top = 0;
+    c->q_tail = c->q_head = c->q_done = 0;
+    c->pending = 0;
+    __threadfence();
+}
 }  // namespace
 
 // Shared-memory carveout for the DFS kernel: the smallest share of the SM's
@@ -2611,6 +2633,90 @@ static cudaError_t l2_persist_setup(int dev, size_t want, size_t* persist, size_
 cudaError_t dfs_blocks_per_sm(int dev, int* occ) {
     int n_sm = 0, occA = 0;
     return device_facts(dev, &n_sm, &occA, occ);
+}
+
+// The status and message for the error a chunk's kernels recorded.
+static mbe_status kernel_error(const Ctrl& hc) {
+    static const char* names[] = {"none",
+                                  "node pool exhausted",
+                                  "task queue full",
+                                  "device wait timed out",
+                                  "search deeper than the frame stack",
+                                  "scratch too small",
+                                  "donated path did not re-derive"};
+    const mbe_status code = hc.error == kErrTimeout ? MBE_ERR_DEVICE_TIMEOUT
+                            : hc.error == kErrPool  ? MBE_ERR_OUT_OF_MEMORY
+                                                    : MBE_ERR_CAPACITY;
+    return fail(code, std::string("enumeration kernel: ") + names[hc.error > 0 && hc.error < 7 ? hc.error : 0] +
+                          " (info " + std::to_string(hc.error_info) + ")");
+}
+
+// engine_run's chunk loop in graph mode (EngineConfig::graph_chunks): every
+// root of a's list, chunk after chunk, with the chunks' kernels (prep, root
+// expansion, DFS; per_launch chunks) captured once into a CUDA graph that
+// is launched until the root cursor has passed the last root.  The scratch
+// must be laid out by the kernels (a.scratch_dyn).  *fall_back is set when
+// a record did not fit the pool (the host-driven loop re-queues such roots
+// and grows the pool); the caller then runs that loop instead.
+static mbe_status run_graph_chunks(EngineBuffers& eb, cudaStream_t s, EngineArgs a, Ctrl* ctrl, Ctrl* pin_ctrl,
+                                   uint32_t n_roots, uint32_t task_cap, uint32_t gridA, uint32_t gridB,
+                                   uint32_t per_launch, cudaEvent_t e0, cudaEvent_t e1, float* ms, uint32_t* chunks,
+                                   bool* fall_back, IoCounters* io) {
+    *fall_back = false;
+    *ms = 0;
+    *chunks = 0;
+    a.roots = (const uint2*)eb.roots.ptr;
+    a.n_roots = n_roots;
+    MBE_CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
+    if (eb.ready_clean < sizeof(uint32_t) * (size_t)task_cap)
+        MBE_CUDA_TRY(cudaMemsetAsync(eb.ready.ptr, 0, sizeof(uint32_t) * (size_t)task_cap, s));
+    eb.ready_clean = 0;  // unknown while the kernels run (the caller restores it after a clean run)
+    eb.cmap_clean = 0;
+    struct Graph {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t x = nullptr;
+        ~Graph() {
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+        }
+    } gr;
+    // nothing between begin and end returns early: a failed capture must
+    // still end, or the stream would stay in capture mode
+    MBE_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t k = 0; k < per_launch; k++) {
+        chunk_prep_kernel<<<1, 32, 0, s>>>(ctrl);
+        expand_roots_kernel<false><<<gridA, kThreadsA, sizeof(uint32_t) * a.stage_words, s>>>(a);
+        dfs_kernel<<<gridB, kThreadsB, 0, s>>>(a);
+    }
+    cudaError_t ce = cudaStreamEndCapture(s, &gr.g);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    MBE_CUDA_TRY(ce);
+    MBE_CUDA_TRY(cudaGraphInstantiate(&gr.x, gr.g, 0));
+    uint32_t last_next = 0;
+    for (;;) {
+        MBE_CUDA_TRY(cudaEventRecord(e0, s));
+        MBE_CUDA_TRY(cudaGraphLaunch(gr.x, s));
+        MBE_CUDA_TRY(cudaEventRecord(e1, s));
+        MBE_CUDA_TRY(cudaMemcpyAsync(pin_ctrl, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+        MBE_CUDA_TRY(cudaStreamSynchronize(s));
+        const Ctrl hc = *pin_ctrl;
+        io->launches += 3 * per_launch;
+        io->d2h += sizeof(Ctrl);
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        *ms += t;
+        *chunks += per_launch;
+        // a record that did not fit (whether or not a later chunk's prep
+        // saw it), or no root claimed in a whole launch: the host loop
+        if (hc.error == kErrPool || hc.n_retry ||
+            (!hc.error && hc.root_next < n_roots && hc.root_next == last_next)) {
+            *fall_back = true;
+            return MBE_OK;
+        }
+        if (hc.error) return kernel_error(hc);
+        if (hc.root_next >= n_roots) return MBE_OK;
+        last_next = hc.root_next;
+    }
 }
 
 mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg,
@@ -2832,7 +2938,9 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         size_t kc = 32;
         while (kc < scr_b) kc <<= 1;
         const size_t bytes = sizeof(uint32_t) * (size_t)nwarpsB * scratch_words(maxW, scr_b, kc, cfg.emit != nullptr);
-        if (ng == 1 && bytes <= (4ull << 30)) {
+        // (graph mode needs it too: no host step between the kernels)
+        const bool want_graph = cfg.graph_chunks && ng > 1 && !cfg.emit && !cfg.mem_cap;
+        if ((ng == 1 || want_graph) && bytes <= (4ull << 30)) {
             if ((st = eb.scratch.ensure(bytes))) return st;
             a.scratch = (uint32_t*)eb.scratch.ptr;
             a.scratch_dyn = 1;
@@ -2888,6 +2996,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
     float ms_a = 0, ms_b = 0;
     uint32_t chunks = 0;
     mbe_status result = MBE_OK;
+    // graph mode: multi-graph runs whose scratch is laid out by the kernels
+    bool use_graph = cfg.graph_chunks && ng > 1 && !cfg.emit && !cfg.mem_cap && a.scratch_dyn;
     for (int attempt = 0;; attempt++) {
         // The node pool grows by doubling when a run exhausts it (up to 60% of
         // free device memory); a fixed cap (cfg.pool_words) disables growth.
@@ -2914,6 +3024,30 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
         // the next chunk (from a host copy), then the main list resumes.
         std::vector<uint2> pending_roots;
         uint32_t main_next = 0;
+        if (use_graph) {
+            // The chunk loop runs on the device: graph_chunks chunks (prep,
+            // root expansion, DFS) captured once into a CUDA graph, launched
+            // until the root cursor has passed every root, with one host
+            // synchronisation per launch instead of two per chunk.
+            bool fall_back = false;
+            result = run_graph_chunks(eb, s, a, ctrl, pin_ctrl, (uint32_t)roots.size(), task_cap, gridA, gridB,
+                                      cfg.graph_chunks, e0, e2, &ms_b, &chunks, &fall_back, io);
+            if (fall_back) {  // a record did not fit the pool: the host loop re-queues it
+                use_graph = false;
+                continue;
+            }
+            if (result != MBE_OK) break;
+            if (results_with_ctrl) {
+                MBE_CUDA_TRY(cudaMemcpyAsync(pin_res, eb.results.ptr, sizeof(ResultAcc) * ng,
+                                             cudaMemcpyDeviceToHost, s));
+                MBE_CUDA_TRY(cudaStreamSynchronize(s));
+                std::memcpy(results.data(), pin_res, sizeof(ResultAcc) * ng);
+                io->d2h += sizeof(ResultAcc) * ng;
+            }
+            eb.ready_clean = sizeof(uint32_t) * (size_t)task_cap;
+            eb.cmap_clean = cmap_known;
+            break;
+        }
         while (main_next < roots.size() || !pending_roots.empty()) {
             chunks++;
             const uint2* list;
@@ -2993,19 +3127,8 @@ mbe_status engine_run(EngineBuffers& eb, cudaStream_t s, const EngineConfig& cfg
                 eb.cmap_clean = cmap_known;
             }
             if (hc.error) {
-                static const char* names[] = {"none",
-                                              "node pool exhausted",
-                                              "task queue full",
-                                              "device wait timed out",
-                                              "search deeper than the frame stack",
-                                              "scratch too small",
-                                              "donated path did not re-derive"};
                 if (hc.error == kErrPool) pool_exhausted = true;
-                mbe_status code = hc.error == kErrTimeout ? MBE_ERR_DEVICE_TIMEOUT
-                                  : hc.error == kErrPool  ? MBE_ERR_OUT_OF_MEMORY
-                                                          : MBE_ERR_CAPACITY;
-                result = fail(code, std::string("enumeration kernel: ") + names[hc.error < 7 ? hc.error : 0] +
-                                        " (info " + std::to_string(hc.error_info) + ")");
+                result = kernel_error(hc);
                 break;
             }
             uint32_t consumed = std::min(hc.root_next, list_n);

@@ -73,6 +73,9 @@ struct EngineConfig {
     uint32_t solve_rows = 32;           // packed records with at most this many rows (<= 32) use the register search
     bool l2_pin = false;                // single-graph, uncapped runs: keep the L-side adjacency persisting in L2
     uint64_t extra_tasks = 1ull << 16;  // ring slots beyond the roots and the margin
+    // Multi-graph runs: chunks captured per CUDA graph launch, the chunk loop
+    // then running on the device (0 = host-driven chunk loop)
+    uint32_t graph_chunks = 8;
     unsigned long long timeout_ns = 60ull * 1000000000ull;
     const EmitTarget* emit = nullptr;
     // Bytes of device memory the run's buffers may hold in total (0 = no

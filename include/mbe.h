@@ -106,10 +106,14 @@ enum {
     MBE_OPT_NO_HASH = 1u << 0,   /* skip the per-biclique canonical hash    */
     MBE_OPT_EMIT = 1u << 1,      /* materialise bicliques into emit buffers */
     MBE_OPT_TIMING = 1u << 2,    /* fill mbe_result.ms with device time     */
-    MBE_OPT_L2_PIN = 1u << 3     /* one-graph runs: keep the graph's L-side
+    MBE_OPT_L2_PIN = 1u << 3,    /* one-graph runs: keep the graph's L-side
                                     adjacency (the lists the root expansion
                                     streams, hubs' included) persisting in
                                     L2 for the run (access-policy window)   */
+    MBE_OPT_HOST_CHUNKS = 1u << 4 /* mbe_batch_run: drive the chunk loop
+                                    from the host (two synchronisations per
+                                    chunk) instead of launching the chunks
+                                    as a captured CUDA graph, the default  */
 };
 
 typedef struct mbe_opts {
