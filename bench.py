@@ -16,7 +16,8 @@ graph.  Prints ONE JSON line (rank 0).
              (host->device copies, transpose, root order), enumerates and
              copies the result back; wall-clock per step.
   roofline   dfs_kernel's algorithmic bytes (4 B x 32-bit words of bit rows
-             and candidate data it streams, counted by the kernel) / its
+             and candidate data it streams, as the kernel's word counter
+             counted them when the per-workload figure was frozen) / its
              event time, against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (a restatement of the reference's search) on
              the host cores over a stride sample of the same graph's roots.
