@@ -261,9 +261,13 @@ MBE_API mbe_status mbe_graph_release(mbe_ctx* ctx, const mbe_graph* g);
 MBE_API mbe_status mbe_enumerate(mbe_ctx* ctx, const mbe_graph* g, mbe_variant variant,
                          const mbe_opts* opts, mbe_result* out);
 
-/* Batched enumeration: n graphs in one persistent launch.  Per-graph
- * results go to out[i].  No reference counterpart: the reference runs one
- * graph per process (src/main.cu:9). */
+/* Batched enumeration: n graphs in one call.  Their roots are expanded in
+ * chunks of ~128 MiB of node records, each chunk enumerated by one
+ * persistent DFS launch; the chunks' launches run as a captured CUDA graph
+ * (8 chunks per graph launch) unless opts->flags has MBE_OPT_HOST_CHUNKS.
+ * Per-graph results go to out[i]; *total_ms (may be NULL) receives the
+ * device time.  No reference counterpart: the reference runs one graph per
+ * process (src/main.cu:9). */
 MBE_API mbe_status mbe_batch_run(mbe_ctx* ctx, const mbe_graph* const* graphs, uint32_t n,
                          mbe_variant variant, const mbe_opts* opts,
                          mbe_result* out, float* total_ms);
