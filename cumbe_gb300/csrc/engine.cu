@@ -390,6 +390,16 @@ __device__ void root_rlist(uint32_t x, const uint32_t* cl, const uint32_t* cntA,
 // L0 (the root's neighbour list) staged in shared memory (dynamic, a.stage_words
 // words per block) when its 16-byte rounded span fits.
 constexpr uint32_t kStageWords = 4096;
+// The two scatters over the neighbours' lists give a warp a whole list; a
+// list longer than kLongList (a hub's) is scanned by the whole block
+// instead, so that one warp's hub list does not keep the other seven
+// waiting at the next barrier.  Up to kLongCap such lists per root are
+// noted (with many long lists the warps' shares even out by themselves);
+// any beyond stay with their warp.  The notes take 260 bytes, so that two
+// root-expansion blocks still fit beside a server slot's three DFS blocks
+// in the DFS kernel's 64 KB carveout.
+constexpr uint32_t kLongList = 128;
+constexpr uint32_t kLongCap = 64;
 
 // kShareSM: the instance capped (server) contexts launch.  Their kernels
 // share SMs with other slots' persistent DFS blocks, so this instance stages
@@ -405,6 +415,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
     __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
     __shared__ unsigned long long s_sabs, s_sl, s_rec, s_scan;
     __shared__ unsigned long long s_keys[2048];
+    __shared__ uint32_t s_long[kLongCap], s_nlong;  // positions in L0 of the long lists
     int* cmap = a.cmap + (size_t)blockIdx.x * a.maxNR;
     uint32_t* cl = a.a_cl + (size_t)blockIdx.x * a.maxNR;
     uint32_t* cntA = a.a_cnt + (size_t)blockIdx.x * a.maxNR;
@@ -431,6 +442,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                     s_idx = i;
             }
             s_ncand = 0;
+            s_nlong = 0;
             s_nq = s_np = s_nabs = s_nonmax = s_counted = 0;
             s_sabs = s_sl = s_scan = 0;
         }
@@ -473,11 +485,32 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
         // 1. candidates C = N(N(x)) \ {x}: first toucher claims a slot.  With
         // the reverse scan the same scatter also counts |N(v) n L0|
         // (src/mbe_cuMBE.cuh:215-227): the per-block map holds touches - 1.
-        unsigned long long scan = 0;
+        unsigned long long scan = 0;  // list entries read (lane 0 / thread 0 counts)
         for (uint32_t j = warp; j < d; j += nwarps) {
             uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
-            scan += e - b;
+            if (e - b > kLongList) {  // noted for the whole block, unless the notes are full
+                uint32_t slot = 0;
+                if (lane == 0) slot = atomicAdd(&s_nlong, 1u);
+                slot = __shfl_sync(kFull, slot, 0);
+                if (slot < kLongCap) {
+                    if (lane == 0) s_long[slot] = j;
+                    continue;
+                }
+            }
+            if (lane == 0) scan += e - b;
             for (uint32_t k = b + lane; k < e; k += 32) {
+                uint32_t v = G.l_adj[k];
+                if (v == x) continue;
+                const int old = rs ? atomicAdd(&cmap[v], 1) : atomicCAS(&cmap[v], -1, -2);
+                if (old == -1) cl[atomicAdd(&s_ncand, 1u)] = v;
+            }
+        }
+        __syncthreads();
+        const uint32_t nlong = min(s_nlong, kLongCap);
+        for (uint32_t h = 0; h < nlong; h++) {
+            const uint32_t u = L0[s_long[h]], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+            if (threadIdx.x == 0) scan += e - b;
+            for (uint32_t k = b + threadIdx.x; k < e; k += blockDim.x) {
                 uint32_t v = G.l_adj[k];
                 if (v == x) continue;
                 const int old = rs ? atomicAdd(&cmap[v], 1) : atomicCAS(&cmap[v], -1, -2);
@@ -510,7 +543,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                     }
                     c += (lo < d && L0[lo] == u);
                 }
-                scan += e - b;
+                if (lane == 0) scan += e - b;
                 c = warp_sum(c);
                 if (lane == 0) cntA[i] = c;
             }
@@ -659,11 +692,26 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                 __syncthreads();
                 // 6. bit rows: bit j of candidate p set iff (L0[j], cand[p]) is an edge
                 if (rs) {
+                    // the long lists noted by the first scatter are scanned
+                    // by the whole block (all of them, when none was left
+                    // with its warp), the rest by a warp each
+                    const bool split = s_nlong <= kLongCap;
                     for (uint32_t j = warp; j < d; j += nwarps) {
                         uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+                        if (split && e - b > kLongList) continue;
                         uint32_t* Mw = M + (size_t)(j >> 5) * n2;
                         uint32_t bit = 1u << (j & 31);
                         for (uint32_t k = b + lane; k < e; k += 32) {
+                            int p = cmap[G.l_adj[k]];
+                            if (p >= 0) atomicOr(&Mw[p], bit);
+                        }
+                    }
+                    for (uint32_t h = 0; split && h < s_nlong; h++) {
+                        const uint32_t j = s_long[h];
+                        const uint32_t u = L0[j], b = G.l_ptr[u], e = G.l_ptr[u + 1];
+                        uint32_t* Mw = M + (size_t)(j >> 5) * n2;
+                        const uint32_t bit = 1u << (j & 31);
+                        for (uint32_t k = b + threadIdx.x; k < e; k += blockDim.x) {
                             int p = cmap[G.l_adj[k]];
                             if (p >= 0) atomicOr(&Mw[p], bit);
                         }
