@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
     extern __shared__ __align__(16) uint32_t s_L0[];
     __shared__ unsigned long long s_bar;
     __shared__ uint32_t s_idx, s_stop, s_ncand, s_nq, s_np, s_nabs, s_nonmax, s_counted;
-    __shared__ uint32_t s_kept[32], s_nk, s_p1, s_nq2, s_wsum[32];
+    __shared__ uint32_t s_kept[32], s_nk, s_p1, s_wsum[32];
     __shared__ unsigned long long s_sabs, s_sl, s_rec, s_scan;
     __shared__ unsigned long long s_keys[2048];
     __shared__ uint32_t s_long[kLongCap], s_nlong;  // positions in L0 of the long lists
@@ -787,27 +787,29 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                 }
                 __syncthreads();
                 PA_MARK(4);
-                // new positions of kept Q rows (block scan in chunks)
-                if (threadIdx.x == 0) s_nq2 = 0;
-                __syncthreads();
-                for (uint32_t b0 = 0; b0 < s_nq; b0 += blockDim.x) {
+                // new positions of kept Q rows (block scan in chunks, one
+                // barrier each: every thread keeps the running total, and
+                // the warp counts alternate between two halves of s_wsum, so
+                // a chunk's counts never overwrite ones still being read)
+                static_assert(kThreadsA / 32 <= 16, "two halves of s_wsum hold the warp counts");
+                uint32_t nq2 = 0;
+                for (uint32_t b0 = 0, it = 0; b0 < s_nq; b0 += blockDim.x, it++) {
+                    uint32_t* ws = s_wsum + (it & 1u) * 16u;
                     uint32_t p = b0 + threadIdx.x;
                     uint32_t f = p < s_nq ? flag[p] : 0u;
                     unsigned bal = __ballot_sync(kFull, f);
-                    if (lane == 0) s_wsum[warp] = __popc(bal);
+                    if (lane == 0) ws[warp] = __popc(bal);
                     __syncthreads();
-                    uint32_t before = s_nq2;
-                    for (uint32_t ww = 0; ww < warp; ww++) before += s_wsum[ww];
-                    if (p < s_nq) flag[p] = f ? (before + __popc(bal & lanemask_lt())) : 0xFFFFFFFFu;
-                    __syncthreads();
-                    if (threadIdx.x == 0) {
-                        uint32_t tot = 0;
-                        for (uint32_t ww = 0; ww < nwarps; ww++) tot += s_wsum[ww];
-                        s_nq2 += tot;
+                    uint32_t before = nq2, tot = 0;
+                    for (uint32_t ww = 0; ww < nwarps; ww++) {
+                        const uint32_t c = ws[ww];
+                        if (ww < warp) before += c;
+                        tot += c;
                     }
-                    __syncthreads();
+                    if (p < s_nq) flag[p] = f ? (before + __popc(bal & lanemask_lt())) : 0xFFFFFFFFu;
+                    nq2 += tot;
                 }
-                const uint32_t nq2 = s_nq2;
+                __syncthreads();  // the new positions are read by other threads below
                 if (nq2 < s_nq) {
                     const uint32_t n3 = nq2 + s_np;
                     // every move goes to a lower address: process arrays in
@@ -836,12 +838,16 @@ __global__ void __launch_bounds__(kThreadsA) expand_roots_kernel(const __grid_co
                                 }
                             }
                             __syncthreads();
+                            // a write lands below its own source, so it can
+                            // only meet sources of lower positions (read by
+                            // now) or of the previous array (done): the next
+                            // chunk's reads need no barrier after the writes
 #pragma unroll
                             for (int q = 0; q < 4; q++)
                                 if (dpos[q] != 0xFFFFFFFFu) dst[dpos[q]] = vals[q];
-                            __syncthreads();
                         }
                     }
+                    __syncthreads();
                     if (threadIdx.x == 0) {
                         NodeHdr* h = (NodeHdr*)rec;
                         h->n = n3;
