@@ -23,6 +23,16 @@ def test_library_exports_every_declared_symbol(built):
     assert declared == set(cm.SIGNATURES), declared ^ set(cm.SIGNATURES)
 
 
+def test_python_option_flags_and_variants_match_the_header():
+    hdr = open(os.path.join(ROOT, "include", "mbe.h")).read()
+    flags = {n: 1 << int(k) for n, k in re.findall(r"MBE_OPT_(\w+)\s*=\s*1u\s*<<\s*(\d+)", hdr)}
+    assert flags, "no option flags parsed"
+    for name, value in flags.items():
+        assert getattr(cm, "OPT_" + name) == value, name
+    variants = {n: int(v) for n, v in re.findall(r"MBE_(CUMBE|NORS|NOES|NOWS)\s*=\s*(\d+)", hdr)}
+    assert {k.upper(): v for k, v in cm.VARIANTS.items()} == variants
+
+
 def test_bi_round_trip_and_normalisation(built, tmp_path):
     # unsorted rows with a duplicate, as data/gen_bi.cpp writes them
     text = "3 4 6\n\n0 3\n3 2\n5 1\n\n2 1\n0 1\n2 1\n3 1\n1 1\n0 1"
